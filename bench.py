@@ -1,0 +1,332 @@
+"""Benchmark: pixel-iterations/s of the perturbation method at 2^-1000 zoom.
+
+Workload (one step = one full frame): 1920x1080 pixels, real-axis width
+2^-1000 around a 1088-bit centre found by seeded ray bisection
+(tests/golden/views.json "c4"), maxiter 200000, Mandelbrot.  A step renders
+the reference orbit on the GPU and every pixel of the frame.
+
+Lines printed (rank 0, one JSON line):
+  value     whole-job pixel-iterations/s with inputs resident on the device
+            (device output buffer), summed over ranks / max step time;
+  e2e       the same metric through the public C ABI call with host output
+            buffers (host->device inputs and device->host counts in the
+            timed region);
+  plain_mp  the plain multi-limb kernel on a band of the same frame (the
+            "perturbation vs plain MP on GPU" half of the metric);
+  roofline  the perturbation kernel against the measured FP32 pipe peak;
+  cpu_baseline  the oracle's MPFR loop (the reference's deep-zoom path at
+            1088 bits) on a bounded pixel sample, all host threads.
+--impl reference times that CPU path alone on the same metric.
+
+Multi-GPU: pixels are independent; every rank renders its own frame (weak
+scaling, no collective on the data path), rank 0 reports the sum.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from fractions import Fraction
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+VIEWS = json.loads((ROOT / "tests" / "golden" / "views.json").read_text())
+ALGO_OPS_PER_PIXEL_ITER = 16   # FP32 ops of one perturbation step
+PLAIN_BAND_ROWS = 8            # rows of the frame rendered by the plain MP kernel
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="c4")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = max(smax, float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def c4_values(view):
+    from mdz_gb300 import MpVal, parse_number
+    prec = int(view["precision"])
+    cx = MpVal.from_fraction(parse_number(view["cx"]), prec)
+    cy = MpVal.from_fraction(parse_number(view["cy"]), prec)
+    width = MpVal.from_fraction(parse_number(view["size"]), prec)
+    return cx, cy, width, prec
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float, op="max") -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(view, seconds: float) -> dict:
+    """The reference's deep-zoom path (per-pixel MPFR loop at the view's
+    precision, src/frac_mandel.c:25-52) on a bounded sample of the frame's
+    pixels, all host threads.  Returns pixel-iterations/s."""
+    from mdz_gb300 import perturb_pixel_c
+    from mdz_gb300.mpval import hexfloat
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    if not O.has_mpfr():
+        return {"value": None, "unit": "pixel-iters/s", "cores": threads, "kind": "port",
+                "sample": "unavailable: libmpfr.so.6 not found on this host"}
+    cx, cy, width, prec = c4_values(view)
+    W, H, depth = view["width"], view["height"], view["depth"]
+    rng = np.random.default_rng(44)
+    done_its, elapsed, n_done = 0, 0.0, 0
+    batch = max(threads, 8)
+    while elapsed < seconds and n_done < 4096:
+        ix = rng.integers(0, W, batch)
+        ln = rng.integers(0, H, batch)
+        cs = [perturb_pixel_c(cx, cy, width, W, H, int(a), int(b)) for a, b in zip(ix, ln)]
+        t0 = time.perf_counter()
+        counts, _ = O.points_mpfr([hexfloat(c[0]) for c in cs], [hexfloat(c[1]) for c in cs],
+                                  depth, prec, threads=threads)
+        elapsed += time.perf_counter() - t0
+        done_its += int(np.where(counts == 0, depth, counts).sum())
+        n_done += batch
+    return {"value": done_its / elapsed, "unit": "pixel-iters/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{n_done} random pixels of the frame, MPFR {prec}-bit loop to depth "
+                      f"{depth}, {elapsed:.1f}s"}
+
+
+def run_reference(args, view, world, rank, dist):
+    if rank != 0:
+        return
+    base = cpu_baseline(view, args.cpu_seconds)
+    vals = []
+    for _ in range(args.steps):
+        b = cpu_baseline(view, max(2.0, args.cpu_seconds / max(1, args.steps)))
+        vals.append(b["value"])
+    value = statistics.median(vals) if vals and vals[0] else None
+    line = {"metric": "pixel-iters/s at 2^-1000 zoom", "impl": "reference", "value": value,
+            "unit": "pixel-iters/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "mpfr-1088", "data": "synthetic",
+            "config": {"workload": "c4: 1920x1080, width 2^-1000, 1088-bit centre, "
+                                   "maxiter 200000, Mandelbrot",
+                       "path": "reference per-pixel MPFR loop (frac_mandel_mpfr) on host cores"},
+            "cpu_baseline": dict(base, value=value),
+            "e2e": {"value": value, "unit": "pixel-iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, view, world, rank, local, dist):
+    import torch
+    from mdz_gb300 import Renderer, native
+    lib = native.load()
+    import ctypes as C
+    cx, cy, width, prec = c4_values(view)
+    W, H, depth = view["width"], view["height"], view["depth"]
+    r = Renderer(local)
+    torch.cuda.set_device(local)
+    d_counts = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
+
+    def step_device():
+        return r.render_perturb_device(W, H, depth, cx, cy, width, prec, d_counts.data_ptr())
+
+    for _ in range(args.warmup):
+        step_device()
+    # measured FP32 pipe peak (roofline denominator)
+    peak = C.c_double()
+    lib.mdzgpu_measure_peak(local, 0, C.byref(peak))
+    torch.cuda.synchronize()
+    barrier(dist)
+    kernel_ms, orbit_ms, its, rebases, wall = [], [], 0, 0, []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = step_device()
+            wall.append((time.perf_counter() - t0) * 1e3)
+            kernel_ms.append(st["kernel_ms"])
+            orbit_ms.append(st["orbit_ms"])
+            its += st["pixel_iters"]
+            rebases += st["rebases"]
+            launches = st["launches"]
+            orbit_len = st["orbit_len"]
+    torch.cuda.synchronize()
+    barrier(dist)
+    total_ms = sum(kernel_ms)
+    total_ms_max = max_over_ranks(dist, total_ms)
+    its_all = max_over_ranks(dist, float(its), op="sum")
+    value = its_all / (total_ms_max * 1e-3)
+
+    # e2e: the public C ABI with host buffers
+    host = np.empty((H, W), np.int32)
+    e2e_ms, e2e_its, h2d, d2h = [], 0, 0, 0
+    barrier(dist)
+    for _ in range(args.steps):
+        flush.fill_(2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, _, st = r.render_perturb(W, H, depth, cx, cy, width, prec, out=host)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e_its += st["pixel_iters"]
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+    e2e_max = max_over_ranks(dist, sum(e2e_ms))
+    e2e_its_all = max_over_ranks(dist, float(e2e_its), op="sum")
+
+    # plain multi-limb kernel on a band of the same frame (same precision)
+    plain = None
+    if not args.no_plain:
+        from mdz_gb300 import MpVal
+        hs = Fraction(width.to_fraction()) / W
+        band = PLAIN_BAND_ROWS
+        y0 = H // 2 - band // 2
+        xmin = MpVal.from_fraction(cx.to_fraction() - W * hs / 2, prec + 64)
+        ymax = MpVal.from_fraction(cy.to_fraction() + (H / 2 - y0) * hs, prec + 64)
+        wv = MpVal.from_fraction(width.to_fraction(), prec + 64)
+        _, pst = r.render_mp(W, band, depth, xmin, ymax, wv, prec, words=34)
+        plain = {"value": pst["pixel_iters"] / (pst["kernel_ms"] * 1e-3),
+                 "unit": "pixel-iters/s", "words": pst["words"],
+                 "sample": f"{W}x{band} band at the frame centre, 34x32-bit words"}
+
+    if rank != 0:
+        r.close()
+        return
+    ms_per_step = total_ms_max / args.steps
+    pert_ms = [k - o for k, o in zip(kernel_ms, orbit_ms)]
+    avg_pert_ms = sum(pert_ms) / len(pert_ms)
+    achieved = (its / args.steps) * ALGO_OPS_PER_PIXEL_ITER / (avg_pert_ms * 1e-3) / 1e9
+    line = {
+        "metric": "pixel-iters/s at 2^-1000 zoom", "value": value, "unit": "pixel-iters/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+int32 floatexp (fp64 rebase)", "data": "synthetic",
+        "config": {"workload": "c4: 1920x1080, width 2^-1000, 1088-bit centre (seeded ray "
+                               "bisection), maxiter 200000, Mandelbrot, perturbation",
+                   "orbit_limbs": int(lib.mdzgpu_perturb_limbs(prec)), "orbit_len": orbit_len,
+                   "l2": "flushed between steps (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": launches * args.steps,
+        "orbit_ms": sum(orbit_ms) / len(orbit_ms),
+        "rebases_per_step": rebases / args.steps,
+        "e2e": {"value": e2e_its_all / (e2e_max * 1e-3), "unit": "pixel-iters/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "fp32-pipe", "achieved": achieved, "peak": peak.value / 1e9,
+                     "unit": "Gop/s", "frac": achieved / (peak.value / 1e9),
+                     "peak_source": "mdzgpu_measure_peak FFMA microbenchmark (this run)",
+                     "traffic": None},
+        "clocks": clocks.summary(),
+        "plain_mp": plain,
+        "perturb_vs_plain": (value / world / plain["value"]) if plain else None,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(view, args.cpu_seconds)
+    r.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    view = VIEWS[args.workload]
+    world, rank, local, dist = dist_init(args)
+    try:
+        if args.impl == "reference":
+            run_reference(args, view, world, rank, dist)
+        else:
+            run_ours(args, view, world, rank, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

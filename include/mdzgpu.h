@@ -1,0 +1,219 @@
+/* libmdzgpu: GB300 (sm_103a) escape-time renderer for MDZ.
+ *
+ * Two layers, both plain C ABI (no CUDA or torch types in any signature):
+ *
+ * 1. Drop-in layer.  The exact entry points of MDZ's render_threads.h and
+ *    fractal.h, so an MDZ build links libmdzgpu in place of
+ *    render_threads.o + fractal.o and its render.c / coords.c / image_info.c
+ *    / palette / GUI code stays unchanged.  rth_ui_start_render renders the
+ *    whole frame on the GPU; the callback installed with rth_set_next_line_cb
+ *    selects the method exactly as image_info_set_multi_prec does
+ *    (src/image_info.c:226-249):
+ *        fractal_calculate_line       -> FP64 kernel (bit-exact with MDZ's
+ *                                        double build without FMA)
+ *        fractal_mpfr_calculate_line  -> multi-limb fixed-point kernel fed
+ *                                        from img->xmin/ymax/width (MPFR)
+ *        fractal_gmp_calculate_line   -> multi-limb fixed-point kernel fed
+ *                                        from img->gxmin/gymax/gwidth (GMP)
+ *    Progress is published row by row through the same lines_rendered /
+ *    lines_drawn protocol, so render.c's progressive colouring works.
+ *
+ * 2. Explicit layer (mdzgpu_*).  Frame renders with explicit parameters,
+ *    host or device output buffers, and the perturbation method; plus the
+ *    serving loop.  Used by the drop-in layer, the tests and bench.py.
+ *
+ * Errors: functions returning int use 0 = MDZGPU_OK, negative = error,
+ * except the drop-in entry points, which keep MDZ's conventions (1 = ok /
+ * 0 = fail, NULL on allocation failure, message on stderr).
+ * mdzgpu_last_error() returns the calling thread's last message. */
+#ifndef MDZGPU_H
+#define MDZGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "mdz_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Drop-in layer: src/render_threads.h:41-87 and src/fractal.h:42-44.  */
+/* ------------------------------------------------------------------ */
+
+/* src/render_threads.h:41 rth_create(): allocates the rthdata and its
+ * private state; NULL on allocation failure. */
+mdz_rthdata* rth_create(void);
+
+/* src/render_threads.h:43 rth_init(): (re)binds img, allocates the
+ * lines_rendered / lines_drawn arrays (user_height entries); 1 ok, 0 fail. */
+int rth_init(mdz_rthdata* rth, int thread_count, int line_draw_count,
+             mdz_image_info* img);
+
+/* src/render_threads.h:54 rth_ui_init(): starts the watch thread that waits
+ * for rth_ui_start_render; 1 ok, 0 fail. */
+int rth_ui_init(mdz_rthdata* rth);
+
+/* src/render_threads.h:55-61: start / stop / quit / timing controls. */
+void rth_ui_start_render(mdz_rthdata* rth);
+void rth_ui_stop_render(mdz_rthdata* rth);
+void rth_ui_stop_render_and_wait(mdz_rthdata* rth);
+void rth_ui_quit(mdz_rthdata* rth);
+void rth_ui_stop_timer(mdz_rthdata* rth);
+void rth_ui_wait_until_started(mdz_rthdata* rth);
+double rth_ui_get_render_time(mdz_rthdata* rth);
+
+/* src/render_threads.h:70: selects the method (see above). */
+void rth_set_next_line_cb(mdz_rthdata* rth,
+                          int (*next_line_cb)(mdz_image_info*, int));
+
+/* src/render_threads.h:83-87: progress protocol, cooperative stop. */
+int rth_process_lines_rendered(mdz_rthdata* rth);
+int rth_render_should_stop(mdz_rthdata* rth);
+int rth_ui_wait_for_line_done(mdz_rthdata* rth);
+
+/* src/fractal.h:42-44: render one real row `line` of img->raw_data on the
+ * GPU.  Return 1 if rendering should continue, 0 if it was stopped. */
+int fractal_calculate_line(mdz_image_info* img, int line);
+int fractal_mpfr_calculate_line(mdz_image_info* img, int line);
+int fractal_gmp_calculate_line(mdz_image_info* img, int line);
+
+/* ------------------------------------------------------------------ */
+/* Explicit layer.                                                     */
+/* ------------------------------------------------------------------ */
+
+enum {
+    MDZGPU_OK = 0,
+    MDZGPU_ERR_ARG = -1,      /* invalid argument */
+    MDZGPU_ERR_CUDA = -2,     /* CUDA runtime error */
+    MDZGPU_ERR_NOMEM = -3,    /* allocation failed */
+    MDZGPU_ERR_RANGE = -4,    /* value outside the fixed-point range */
+    MDZGPU_ERR_STOPPED = -5,  /* stopped through the stop word */
+    MDZGPU_ERR_TIMEOUT = -6,  /* a bounded device wait gave up */
+    MDZGPU_ERR_UNSUPPORTED = -7
+};
+
+typedef struct mdzgpu_ctx mdzgpu_ctx;
+
+/* Context = one CUDA device, one stream and the reusable device buffers. */
+mdzgpu_ctx* mdzgpu_create(int device);
+void mdzgpu_destroy(mdzgpu_ctx* ctx);
+const char* mdzgpu_last_error(void);
+const char* mdzgpu_version(void);
+
+/* Frame geometry: the REAL (supersampled) size, as img->real_width/height. */
+typedef struct mdzgpu_frame {
+    int32_t width;
+    int32_t height;
+    int32_t family;   /* MDZ_FAMILY_MANDEL / MDZ_FAMILY_JULIA */
+    int32_t fractal;  /* MDZ_MANDELBROT .. MDZ_VARIANT */
+    int64_t depth;    /* maximum iterations, 1 .. INT32_MAX */
+} mdzgpu_frame;
+
+/* Filled by every render call (may be NULL). */
+typedef struct mdzgpu_stats {
+    double kernel_ms;       /* device time of the render kernels (events) */
+    double wall_ms;         /* host wall time of the whole call */
+    int64_t pixel_iters;    /* sum over pixels of (count ? count : depth) */
+    int64_t h2d_bytes;      /* host->device bytes copied by the call */
+    int64_t d2h_bytes;      /* device->host bytes copied by the call */
+    int32_t launches;       /* kernels launched by the call */
+    int32_t words;          /* 32-bit words per fixed-point number (MP) */
+    double orbit_ms;        /* reference-orbit kernel time (perturbation) */
+    int64_t rebases;        /* rebases taken (perturbation) */
+    int64_t orbit_len;      /* reference orbit length (perturbation) */
+} mdzgpu_stats;
+
+/* An arbitrary-precision binary value with MPFR's meaning:
+ *   value = sign * 0.d[n-1] d[n-2] ... d[0] (binary) * 2^exp,
+ * limbs least significant first, d[n-1] normalised (top bit set).
+ * n == 0 or d == NULL means zero. */
+typedef struct mdzgpu_mpval {
+    int32_t sign;
+    int32_t nlimbs;
+    int64_t exp;
+    const uint64_t* d;
+} mdzgpu_mpval;
+
+/* FP64 path (the fractal_calculate_line arithmetic, src/fractal.c:29-117):
+ * width = xmax - xmin; y = ymax - (width/W)*line; x = (ix/W)*width + xmin,
+ * each an IEEE double operation with round-to-nearest and no contraction.
+ * counts: host buffer of width*height int32 (row-major); a count is the
+ * first iteration with |z|^2 > 4, or 0 if not escaped within depth. */
+int mdzgpu_render_fp64(mdzgpu_ctx* ctx, const mdzgpu_frame* f, double xmin,
+                       double xmax, double ymax, double julia_re,
+                       double julia_im, int32_t* counts, mdzgpu_stats* st);
+/* Same, output left in device memory (d_counts, width*height int32). */
+int mdzgpu_render_fp64_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
+                              double xmin, double xmax, double ymax,
+                              double julia_re, double julia_im,
+                              int32_t* d_counts, mdzgpu_stats* st);
+
+/* Multi-limb fixed-point path (fractal_mpfr_calculate_line geometry,
+ * src/fractal.c:159-192): x = xmin + ix*width/W, y = ymax - line*width/W.
+ * `words` = 32-bit words per number (0 = choose from `precision`: the
+ * smallest even count with at least precision+8 bits); the number has
+ * 32*words-8 fractional bits.  |coordinates| must be < 4. */
+int mdzgpu_render_mp(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
+                     const mdzgpu_mpval* xmin, const mdzgpu_mpval* ymax,
+                     const mdzgpu_mpval* width, const mdzgpu_mpval* julia_re,
+                     const mdzgpu_mpval* julia_im, int64_t precision,
+                     int32_t words, int32_t* counts, mdzgpu_stats* st);
+int mdzgpu_render_mp_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
+                            const mdzgpu_mpval* xmin, const mdzgpu_mpval* ymax,
+                            const mdzgpu_mpval* width,
+                            const mdzgpu_mpval* julia_re,
+                            const mdzgpu_mpval* julia_im, int64_t precision,
+                            int32_t words, int32_t* d_counts,
+                            mdzgpu_stats* st);
+/* Largest `words` value the MP kernel is built for. */
+int32_t mdzgpu_mp_max_words(void);
+
+/* Perturbation path (new method; the reference has none).  Renders the
+ * Mandelbrot family/formula around the centre (cx, cy) with real-axis
+ * `width`: pixel (ix, line) is c = (cx + (2 ix - W) hs, cy + (H - 2 line) hs)
+ * where hs = width / (2 W) rounded to 40 significant bits (exactly the value
+ * mdzgpu_perturb_spacing returns; this is MDZ's centre/size geometry,
+ * src/coords.c:265-302, with square pixels).  One reference orbit of the
+ * centre is iterated on the GPU in `limbs` radix-2^28 digits (0 = choose
+ * from `precision`: ceil(precision / 28) + 1), then every pixel runs in
+ * FP32-mantissa / int32-exponent deltas with FP64 rebasing.  counts as in
+ * the other paths; mag2 (nullable) receives |z|^2 at escape in FP32, for
+ * smooth colouring. */
+int mdzgpu_render_perturb(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
+                          const mdzgpu_mpval* cx, const mdzgpu_mpval* cy,
+                          const mdzgpu_mpval* width, int64_t precision,
+                          int32_t limbs, int32_t* counts, float* mag2,
+                          mdzgpu_stats* st);
+int mdzgpu_render_perturb_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
+                                 const mdzgpu_mpval* cx,
+                                 const mdzgpu_mpval* cy,
+                                 const mdzgpu_mpval* width, int64_t precision,
+                                 int32_t limbs, int32_t* d_counts,
+                                 float* d_mag2, mdzgpu_stats* st);
+/* Half pixel spacing used by the perturbation path: width/(2W) = hs_m 2^hs_e
+ * with hs_m in [1, 2) holding at most 40 significant bits. */
+int mdzgpu_perturb_spacing(const mdzgpu_mpval* width, int32_t W,
+                           double* hs_m, int32_t* hs_e);
+/* Orbit digits chosen for a precision (ceil(precision / 28) + 1, >= 5). */
+int32_t mdzgpu_perturb_limbs(int64_t precision);
+
+/* Fixed-point helpers exposed for tests: convert an mpval to the kernel's
+ * fixed-point words (out has `words` entries); 0 ok, MDZGPU_ERR_RANGE. */
+int mdzgpu_fx_from_mpval(const mdzgpu_mpval* v, int32_t words, uint32_t* out);
+
+/* Measured pipe throughput of `device` in operations per second, the
+ * roofline denominators of these compute-bound kernels: kind 0 = FP32 FFMA,
+ * 1 = INT32 IMAD (mad.lo.u32), 2 = FP64 DMUL/DADD (unfused). */
+int mdzgpu_measure_peak(int device, int kind, double* ops_per_s);
+
+/* Writes offsetof() of every mdz_image_info / mdz_rthdata field, in
+ * declaration order, into out (capacity n); returns the count written.
+ * Used to check the drop-in ABI against MDZ's own headers. */
+int mdzgpu_abi_layout(int64_t* out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

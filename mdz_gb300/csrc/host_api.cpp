@@ -1,0 +1,714 @@
+// Explicit-parameter C ABI of libmdzgpu (mdzgpu_*): contexts, frame renders
+// for the FP64, multi-limb and perturbation methods.
+#include <math.h>
+#include <stdarg.h>
+#include <stddef.h>
+#include <string.h>
+
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace mdz {
+
+namespace {
+thread_local std::string g_last_error;
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+int validate_frame(const mdzgpu_frame* f)
+{
+    if (!f || f->width <= 0 || f->height <= 0 || f->width > 1 << 20 || f->height > 1 << 20) {
+        set_error("invalid frame size");
+        return MDZGPU_ERR_ARG;
+    }
+    if (f->depth < 1 || f->depth > 0x7fffffffLL) {
+        set_error("depth %lld outside [1, INT32_MAX]", (long long)f->depth);
+        return MDZGPU_ERR_ARG;
+    }
+    if (f->family != MDZ_FAMILY_MANDEL && f->family != MDZ_FAMILY_JULIA) {
+        set_error("unknown family %d", f->family);
+        return MDZGPU_ERR_ARG;
+    }
+    return MDZGPU_OK;
+}
+
+struct Timing {
+    double t0;
+    explicit Timing() : t0(now_ms()) {}
+};
+
+}  // namespace
+
+void set_error(const char* fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    fprintf(stderr, "mdzgpu: %s\n", buf);
+}
+
+int DevBuf::ensure(size_t want)
+{
+    if (want <= bytes && ptr)
+        return MDZGPU_OK;
+    release();
+    size_t b = want < 256 ? 256 : want;
+    cudaError_t e = cudaMalloc(&ptr, b);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        set_error("cudaMalloc(%zu): %s", b, cudaGetErrorString(e));
+        return MDZGPU_ERR_NOMEM;
+    }
+    bytes = b;
+    return MDZGPU_OK;
+}
+
+void DevBuf::release()
+{
+    if (ptr)
+        cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+int PinnedBuf::ensure(size_t want)
+{
+    if (want <= bytes && host)
+        return MDZGPU_OK;
+    release();
+    size_t b = want < 4096 ? 4096 : want;
+    cudaError_t e = cudaHostAlloc(&host, b, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        host = nullptr;
+        set_error("cudaHostAlloc(%zu): %s", b, cudaGetErrorString(e));
+        return MDZGPU_ERR_NOMEM;
+    }
+    e = cudaHostGetDevicePointer(&dev, host, 0);
+    if (e != cudaSuccess) {
+        cudaFreeHost(host);
+        host = nullptr;
+        set_error("cudaHostGetDevicePointer: %s", cudaGetErrorString(e));
+        return MDZGPU_ERR_CUDA;
+    }
+    bytes = b;
+    return MDZGPU_OK;
+}
+
+void PinnedBuf::release()
+{
+    if (host)
+        cudaFreeHost(host);
+    host = nullptr;
+    dev = nullptr;
+    bytes = 0;
+}
+
+int digits28_from_mpval(const mdzgpu_mpval* v, int L, int* out)
+{
+    // magnitude bits -> unsigned digits, then balance to [-2^27, 2^27)
+    const long F = 28L * (L - 1);
+    std::vector<long long> d(L + 1, 0);
+    if (v && v->d && v->nlimbs > 0) {
+        const long shift = (long)v->exp - 64L * v->nlimbs + F;
+        for (int i = 0; i < v->nlimbs; ++i) {
+            const uint64_t limb = v->d[i];
+            for (int b = 0; b < 64; ++b) {
+                if (!((limb >> b) & 1u))
+                    continue;
+                const long pos = (long)i * 64 + b + shift;
+                if (pos < 0)
+                    continue;
+                if (pos >= 28L * L - 3)
+                    return MDZGPU_ERR_RANGE;
+                d[pos / 28] |= 1ll << (pos % 28);
+            }
+        }
+    }
+    if (v && v->sign < 0)
+        for (auto& x : d)
+            x = -x;
+    for (int i = 0; i < L; ++i) {
+        const long long digit = ((d[i] + (1ll << 27)) & ((1ll << 28) - 1)) - (1ll << 27);
+        const long long carry = (d[i] - digit) >> 28;
+        d[i] = digit;
+        d[i + 1] += carry;
+    }
+    if (d[L] != 0)
+        return MDZGPU_ERR_RANGE;
+    for (int i = 0; i < L; ++i)
+        out[i] = (int)d[i];
+    return MDZGPU_OK;
+}
+
+int half_spacing(const mdzgpu_mpval* width, int W, double* hs_m, int* hs_e)
+{
+    if (!width || !width->d || width->nlimbs <= 0 || W <= 0) {
+        set_error("perturbation needs a positive width");
+        return MDZGPU_ERR_ARG;
+    }
+    // top 53 bits of the mantissa, as an integer-valued double
+    const uint64_t top = width->d[width->nlimbs - 1];
+    const double mant = (double)(top >> 11);            // exact, 53 bits
+    const long e0 = (long)width->exp - 53;              // width ~ mant * 2^e0
+    double q = mant / (2.0 * (double)W);
+    const int k = ilogb(q);
+    double m = ldexp(q, -k);                            // [1, 2)
+    m = ldexp(nearbyint(ldexp(m, 39)), -39);            // 40 significant bits
+    *hs_m = m;
+    *hs_e = (int)(e0 + k);
+    return MDZGPU_OK;
+}
+
+}  // namespace mdz
+
+using namespace mdz;
+
+extern "C" {
+
+const char* mdzgpu_last_error(void)
+{
+    return g_last_error.c_str();
+}
+
+const char* mdzgpu_version(void)
+{
+    return "mdzgpu 0.1 (sm_103a)";
+}
+
+mdzgpu_ctx* mdzgpu_create(int device)
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n <= device || device < 0) {
+        set_error("no CUDA device %d (%s)", device, cudaGetErrorString(e));
+        return nullptr;
+    }
+    if ((e = cudaSetDevice(device)) != cudaSuccess) {
+        set_error("cudaSetDevice: %s", cudaGetErrorString(e));
+        return nullptr;
+    }
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, device)) != cudaSuccess) {
+        set_error("cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+        return nullptr;
+    }
+    auto* ctx = new mdzgpu_ctx();
+    ctx->device = device;
+    ctx->num_sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess
+        || cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        set_error("stream/event creation failed");
+        delete ctx;
+        return nullptr;
+    }
+    return ctx;
+}
+
+void mdzgpu_destroy(mdzgpu_ctx* ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->counts.release();
+    ctx->sync.release();
+    ctx->coords.release();
+    ctx->orbit.release();
+    ctx->orbit_fx.release();
+    ctx->aux.release();
+    ctx->pinned.release();
+    ctx->staging.release();
+    cudaEventDestroy(ctx->ev0);
+    cudaEventDestroy(ctx->ev1);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+static int finish_stats(mdzgpu_ctx* ctx, mdzgpu_stats* st, double t0, int launches,
+                        int64_t h2d, int64_t d2h)
+{
+    FrameSync hs;
+    MDZ_CUDA_TRY(cudaMemcpyAsync(&hs, ctx->sync.ptr, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream));
+    MDZ_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (st) {
+        float ms = 0.f;
+        MDZ_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        st->kernel_ms = ms;
+        st->pixel_iters = (int64_t)hs.iter_sum;
+        st->launches = launches;
+        st->h2d_bytes = h2d;
+        st->d2h_bytes = d2h + (int64_t)sizeof hs;
+        st->wall_ms = now_ms() - t0;
+    }
+    return MDZGPU_OK;
+}
+
+static int fp64_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, double xmin, double xmax,
+                       double ymax, double jre, double jim, int32_t* d_out, int32_t* h_out,
+                       mdzgpu_stats* st)
+{
+    const double t0 = now_ms();
+    if (!ctx) {
+        set_error("null context");
+        return MDZGPU_ERR_ARG;
+    }
+    int rc = validate_frame(f);
+    if (rc)
+        return rc;
+    MDZ_CUDA_TRY(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)f->width * f->height;
+    if (!d_out) {
+        if ((rc = ctx->counts.ensure(n * sizeof(int32_t))))
+            return rc;
+        d_out = (int32_t*)ctx->counts.ptr;
+    }
+    if ((rc = ctx->sync.ensure(sizeof(FrameSync))))
+        return rc;
+    if (st)
+        memset(st, 0, sizeof *st);
+    MDZ_CUDA_TRY(cudaMemsetAsync(ctx->sync.ptr, 0, sizeof(FrameSync), ctx->stream));
+    Fp64Launch p;
+    p.W = f->width;
+    p.H = f->height;
+    p.row0 = 0;
+    p.nrows = f->height;
+    p.family = f->family;
+    p.fractal = f->fractal;
+    p.depth = (uint32_t)f->depth;
+    p.xmin = xmin;
+    p.xmax = xmax;
+    p.ymax = ymax;
+    p.jre = jre;
+    p.jim = jim;
+    p.out = d_out;
+    p.sync = (FrameSync*)ctx->sync.ptr;
+    p.tile_rows_done = nullptr;
+    p.band_flags = nullptr;
+    p.stop = nullptr;
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+    if ((rc = launch_fp64(ctx, p, ctx->stream)))
+        return rc;
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
+    int64_t d2h = 0;
+    if (h_out) {
+        MDZ_CUDA_TRY(cudaMemcpyAsync(h_out, d_out, n * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        d2h = (int64_t)(n * sizeof(int32_t));
+    }
+    return finish_stats(ctx, st, t0, 1, 0, d2h);
+}
+
+int mdzgpu_render_fp64(mdzgpu_ctx* ctx, const mdzgpu_frame* f, double xmin, double xmax,
+                       double ymax, double julia_re, double julia_im, int32_t* counts,
+                       mdzgpu_stats* st)
+{
+    if (!counts) {
+        set_error("null counts buffer");
+        return MDZGPU_ERR_ARG;
+    }
+    return fp64_common(ctx, f, xmin, xmax, ymax, julia_re, julia_im, nullptr, counts, st);
+}
+
+int mdzgpu_render_fp64_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f, double xmin,
+                              double xmax, double ymax, double julia_re, double julia_im,
+                              int32_t* d_counts, mdzgpu_stats* st)
+{
+    if (!d_counts) {
+        set_error("null device counts buffer");
+        return MDZGPU_ERR_ARG;
+    }
+    return fp64_common(ctx, f, xmin, xmax, ymax, julia_re, julia_im, d_counts, nullptr, st);
+}
+
+int32_t mdzgpu_mp_max_words(void)
+{
+    return 36;
+}
+
+static int pick_words(long precision, int words)
+{
+    if (words <= 0)
+        words = mp_words_for_precision(precision);
+    for (int w = words; w <= mdzgpu_mp_max_words(); ++w)
+        if (mp_words_supported(w))
+            return w;
+    return -1;
+}
+
+// Builds the fixed-point x / y tables of a frame on the host:
+//   x[ix]   = xmin + ix * width / W
+//   y[line] = ymax - line * width / W
+static int mp_tables(const uint32_t* xmin, const uint32_t* ymax, const uint32_t* width, int W,
+                     int H, int words, std::vector<uint32_t>& tab)
+{
+    tab.assign((size_t)(W + H) * words, 0);
+    for (int ix = 0; ix < W; ++ix) {
+        uint32_t* o = &tab[(size_t)ix * words];
+        fx_affine(xmin, width, ix, W, +1, words, o);
+        if (!fx_fits_coordinate(o, words))
+            return MDZGPU_ERR_RANGE;
+    }
+    for (int y = 0; y < H; ++y) {
+        uint32_t* o = &tab[(size_t)(W + y) * words];
+        fx_affine(ymax, width, y, W, -1, words, o);
+        if (!fx_fits_coordinate(o, words))
+            return MDZGPU_ERR_RANGE;
+    }
+    return MDZGPU_OK;
+}
+
+}  // extern "C"
+
+namespace mdz {
+
+int mp_render_fixed(mdzgpu_ctx* ctx, const mdzgpu_frame* f, int words, const uint32_t* fxmin,
+                    const uint32_t* fymax, const uint32_t* fwidth, const uint32_t* fjre,
+                    const uint32_t* fjim, int32_t* d_out, int32_t* h_out, mdzgpu_stats* st,
+                    double t0)
+{
+    int rc;
+    const int W = f->width, H = f->height;
+    std::vector<uint32_t> tab;
+    if ((rc = mp_tables(fxmin, fymax, fwidth, W, H, words, tab))) {
+        set_error("multi-limb path: coordinates must satisfy |x|, |y| < 4");
+        return rc;
+    }
+    tab.resize(tab.size() + 2 * (size_t)words);
+    memcpy(&tab[(size_t)(W + H) * words], fjre, words * sizeof(uint32_t));
+    memcpy(&tab[(size_t)(W + H + 1) * words], fjim, words * sizeof(uint32_t));
+    if (f->family == MDZ_FAMILY_JULIA && (!fx_fits_coordinate(fjre, words) || !fx_fits_coordinate(fjim, words))) {
+        set_error("multi-limb path: julia constant must satisfy |c| < 4");
+        return MDZGPU_ERR_RANGE;
+    }
+    const size_t n = (size_t)W * H;
+    if (!d_out) {
+        if ((rc = ctx->counts.ensure(n * sizeof(int32_t))))
+            return rc;
+        d_out = (int32_t*)ctx->counts.ptr;
+    }
+    if ((rc = ctx->sync.ensure(sizeof(FrameSync))) || (rc = ctx->coords.ensure(tab.size() * 4)))
+        return rc;
+    if (st)
+        memset(st, 0, sizeof *st);
+    MDZ_CUDA_TRY(cudaMemcpyAsync(ctx->coords.ptr, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    MDZ_CUDA_TRY(cudaMemsetAsync(ctx->sync.ptr, 0, sizeof(FrameSync), ctx->stream));
+    MpLaunch p;
+    p.W = W;
+    p.H = H;
+    p.row0 = 0;
+    p.nrows = H;
+    p.family = f->family;
+    p.fractal = f->fractal;
+    p.depth = (uint32_t)f->depth;
+    p.words = words;
+    p.xs = (const uint32_t*)ctx->coords.ptr;
+    p.ys = p.xs + (size_t)W * words;
+    p.julia = p.xs + (size_t)(W + H) * words;
+    p.out = d_out;
+    p.sync = (FrameSync*)ctx->sync.ptr;
+    p.tile_rows_done = nullptr;
+    p.band_flags = nullptr;
+    p.stop = nullptr;
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+    if ((rc = launch_mp(ctx, p, ctx->stream)))
+        return rc;
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
+    int64_t d2h = 0;
+    if (h_out) {
+        MDZ_CUDA_TRY(cudaMemcpyAsync(h_out, d_out, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        d2h = (int64_t)n * 4;
+    }
+    rc = finish_stats(ctx, st, t0, 1, (int64_t)tab.size() * 4, d2h);
+    if (st)
+        st->words = words;
+    return rc;
+}
+
+}  // namespace mdz
+
+extern "C" {
+
+static int mp_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* xmin,
+                     const mdzgpu_mpval* ymax, const mdzgpu_mpval* width,
+                     const mdzgpu_mpval* jre, const mdzgpu_mpval* jim, int64_t precision,
+                     int32_t words, int32_t* d_out, int32_t* h_out, mdzgpu_stats* st)
+{
+    const double t0 = now_ms();
+    if (!ctx) {
+        set_error("null context");
+        return MDZGPU_ERR_ARG;
+    }
+    int rc = validate_frame(f);
+    if (rc)
+        return rc;
+    MDZ_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int w = pick_words((long)precision, words);
+    if (w < 0) {
+        set_error("precision %lld needs more than %d words", (long long)precision,
+                  mdzgpu_mp_max_words());
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    std::vector<uint32_t> a(w), b(w), c(w), jr(w), ji(w);
+    if (fx_from_mpval(xmin, w, a.data()) || fx_from_mpval(ymax, w, b.data())
+        || fx_from_mpval(width, w, c.data()) || fx_from_mpval(jre, w, jr.data())
+        || fx_from_mpval(jim, w, ji.data())) {
+        set_error("multi-limb path: value outside the fixed-point range");
+        return MDZGPU_ERR_RANGE;
+    }
+    return mp_render_fixed(ctx, f, w, a.data(), b.data(), c.data(), jr.data(), ji.data(), d_out,
+                           h_out, st, t0);
+}
+
+int mdzgpu_render_mp(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* xmin,
+                     const mdzgpu_mpval* ymax, const mdzgpu_mpval* width,
+                     const mdzgpu_mpval* julia_re, const mdzgpu_mpval* julia_im,
+                     int64_t precision, int32_t words, int32_t* counts, mdzgpu_stats* st)
+{
+    if (!counts) {
+        set_error("null counts buffer");
+        return MDZGPU_ERR_ARG;
+    }
+    return mp_common(ctx, f, xmin, ymax, width, julia_re, julia_im, precision, words, nullptr,
+                     counts, st);
+}
+
+int mdzgpu_render_mp_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* xmin,
+                            const mdzgpu_mpval* ymax, const mdzgpu_mpval* width,
+                            const mdzgpu_mpval* julia_re, const mdzgpu_mpval* julia_im,
+                            int64_t precision, int32_t words, int32_t* d_counts,
+                            mdzgpu_stats* st)
+{
+    if (!d_counts) {
+        set_error("null device counts buffer");
+        return MDZGPU_ERR_ARG;
+    }
+    return mp_common(ctx, f, xmin, ymax, width, julia_re, julia_im, precision, words, d_counts,
+                     nullptr, st);
+}
+
+int mdzgpu_fx_from_mpval(const mdzgpu_mpval* v, int32_t words, uint32_t* out)
+{
+    if (!out || words < 2)
+        return MDZGPU_ERR_ARG;
+    return fx_from_mpval(v, words, out);
+}
+
+int mdzgpu_perturb_spacing(const mdzgpu_mpval* width, int32_t W, double* hs_m, int32_t* hs_e)
+{
+    int e = 0;
+    int rc = half_spacing(width, W, hs_m, &e);
+    if (hs_e)
+        *hs_e = e;
+    return rc;
+}
+
+int32_t mdzgpu_perturb_limbs(int64_t precision)
+{
+    long L = (long)((precision + 27) / 28) + 1;
+    if (L < 5)
+        L = 5;
+    return (int32_t)L;
+}
+
+static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,
+                          const mdzgpu_mpval* cy, const mdzgpu_mpval* width, int64_t precision,
+                          int32_t limbs, int32_t* d_out, float* d_mag, int32_t* h_out,
+                          float* h_mag, mdzgpu_stats* st)
+{
+    const double t0 = now_ms();
+    if (!ctx) {
+        set_error("null context");
+        return MDZGPU_ERR_ARG;
+    }
+    int rc = validate_frame(f);
+    if (rc)
+        return rc;
+    if (f->family != MDZ_FAMILY_MANDEL || f->fractal != MDZ_MANDELBROT) {
+        set_error("perturbation: only the Mandelbrot family / formula is implemented");
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    MDZ_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int L = limbs > 0 ? limbs : mdzgpu_perturb_limbs(precision);
+    if (L > orbit_max_limbs() || L < 5) {
+        set_error("perturbation: %d orbit limbs outside [5, %d]", L, orbit_max_limbs());
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    std::vector<int> dig(2 * (size_t)L);
+    if (digits28_from_mpval(cx, L, dig.data()) || digits28_from_mpval(cy, L, dig.data() + L)) {
+        set_error("perturbation: centre outside the fixed-point range");
+        return MDZGPU_ERR_RANGE;
+    }
+    if (abs(dig[L - 1]) >= 4 || abs(dig[2 * L - 1]) >= 4) {
+        set_error("perturbation: centre must satisfy |cx|, |cy| < 4");
+        return MDZGPU_ERR_RANGE;
+    }
+    double hs_m = 0.0;
+    int hs_e = 0;
+    if ((rc = half_spacing(width, f->width, &hs_m, &hs_e)))
+        return rc;
+    const size_t n = (size_t)f->width * f->height;
+    const size_t entries = (size_t)f->depth + 2;
+    // orbit layout: zf[entries] float2 | zd[entries] double2 | ze[entries] int | len
+    const size_t off_zd = ((entries * sizeof(float2)) + 255) & ~(size_t)255;
+    const size_t off_ze = off_zd + (((entries * sizeof(double2)) + 255) & ~(size_t)255);
+    const size_t off_len = off_ze + (((entries * sizeof(int)) + 255) & ~(size_t)255);
+    const size_t off_dig = off_len + 256;
+    const size_t off_reb = off_dig + ((2 * L * sizeof(int) + 255) & ~(size_t)255);
+    const size_t orbit_bytes = off_reb + 256;
+    if ((rc = ctx->orbit.ensure(orbit_bytes)) || (rc = ctx->sync.ensure(sizeof(FrameSync))))
+        return rc;
+    if (!d_out) {
+        if ((rc = ctx->counts.ensure(n * sizeof(int32_t))))
+            return rc;
+        d_out = (int32_t*)ctx->counts.ptr;
+    }
+    if (!d_mag && h_mag) {
+        if ((rc = ctx->aux.ensure(n * sizeof(float))))
+            return rc;
+        d_mag = (float*)ctx->aux.ptr;
+    }
+    if (st)
+        memset(st, 0, sizeof *st);
+    char* ob = (char*)ctx->orbit.ptr;
+    MDZ_CUDA_TRY(cudaMemcpyAsync(ob + off_dig, dig.data(), dig.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    MDZ_CUDA_TRY(cudaMemsetAsync(ob + off_reb, 0, 256, ctx->stream));
+    MDZ_CUDA_TRY(cudaMemsetAsync(ctx->sync.ptr, 0, sizeof(FrameSync), ctx->stream));
+    OrbitLaunch o;
+    o.limbs = L;
+    o.c_re = (const int*)(ob + off_dig);
+    o.c_im = o.c_re + L;
+    o.zf = (float2*)ob;
+    o.zd = (double2*)(ob + off_zd);
+    o.ze = (int*)(ob + off_ze);
+    o.max_k = (int)f->depth + 1;
+    o.out_len = (int*)(ob + off_len);
+    cudaEvent_t evo;
+    MDZ_CUDA_TRY(cudaEventCreate(&evo));
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+    if ((rc = launch_orbit(o, ctx->stream))) {
+        cudaEventDestroy(evo);
+        return rc;
+    }
+    MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->stream));
+    PerturbLaunch p;
+    p.W = f->width;
+    p.H = f->height;
+    p.row0 = 0;
+    p.nrows = f->height;
+    p.depth = (uint32_t)f->depth;
+    p.hs_m = hs_m;
+    p.hs_e = hs_e;
+    p.zf = o.zf;
+    p.zd = o.zd;
+    p.ze = o.ze;
+    p.orbit_len = o.out_len;
+    p.out = d_out;
+    p.mag = d_mag;
+    p.sync = (FrameSync*)ctx->sync.ptr;
+    p.rebases = (unsigned long long*)(ob + off_reb);
+    p.stop = nullptr;
+    if ((rc = launch_perturb(ctx, p, ctx->stream))) {
+        cudaEventDestroy(evo);
+        return rc;
+    }
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
+    int64_t d2h = 0;
+    if (h_out) {
+        MDZ_CUDA_TRY(cudaMemcpyAsync(h_out, d_out, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        d2h += (int64_t)n * 4;
+    }
+    if (h_mag) {
+        MDZ_CUDA_TRY(cudaMemcpyAsync(h_mag, d_mag, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        d2h += (int64_t)n * 4;
+    }
+    unsigned long long reb = 0;
+    int olen = 0;
+    MDZ_CUDA_TRY(cudaMemcpyAsync(&reb, p.rebases, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    MDZ_CUDA_TRY(cudaMemcpyAsync(&olen, o.out_len, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    rc = finish_stats(ctx, st, t0, 2, (int64_t)dig.size() * 4, d2h + 12);
+    if (!rc && st) {
+        float oms = 0.f;
+        cudaEventElapsedTime(&oms, ctx->ev0, evo);
+        st->orbit_ms = oms;
+        st->rebases = (int64_t)reb;
+        st->orbit_len = olen;
+    }
+    cudaEventDestroy(evo);
+    return rc;
+}
+
+int mdzgpu_render_perturb(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,
+                          const mdzgpu_mpval* cy, const mdzgpu_mpval* width, int64_t precision,
+                          int32_t limbs, int32_t* counts, float* mag2, mdzgpu_stats* st)
+{
+    if (!counts) {
+        set_error("null counts buffer");
+        return MDZGPU_ERR_ARG;
+    }
+    return perturb_common(ctx, f, cx, cy, width, precision, limbs, nullptr, nullptr, counts, mag2,
+                          st);
+}
+
+int mdzgpu_render_perturb_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
+                                 const mdzgpu_mpval* cx, const mdzgpu_mpval* cy,
+                                 const mdzgpu_mpval* width, int64_t precision, int32_t limbs,
+                                 int32_t* d_counts, float* d_mag2, mdzgpu_stats* st)
+{
+    if (!d_counts) {
+        set_error("null device counts buffer");
+        return MDZGPU_ERR_ARG;
+    }
+    return perturb_common(ctx, f, cx, cy, width, precision, limbs, d_counts, d_mag2, nullptr,
+                          nullptr, st);
+}
+
+int mdzgpu_abi_layout(int64_t* out, int n)
+{
+    const int64_t offs[] = {
+        (int64_t)offsetof(mdz_image_info, xmin),        (int64_t)offsetof(mdz_image_info, xmax),
+        (int64_t)offsetof(mdz_image_info, ymax),        (int64_t)offsetof(mdz_image_info, width),
+        (int64_t)offsetof(mdz_image_info, gxmin),       (int64_t)offsetof(mdz_image_info, gxmax),
+        (int64_t)offsetof(mdz_image_info, gymax),       (int64_t)offsetof(mdz_image_info, gwidth),
+        (int64_t)offsetof(mdz_image_info, old_cx),      (int64_t)offsetof(mdz_image_info, old_cy),
+        (int64_t)offsetof(mdz_image_info, old_size),    (int64_t)offsetof(mdz_image_info, pcoords),
+        (int64_t)offsetof(mdz_image_info, depth),       (int64_t)offsetof(mdz_image_info, thread_count),
+        (int64_t)offsetof(mdz_image_info, draw_lines),  (int64_t)offsetof(mdz_image_info, raw_data),
+        (int64_t)offsetof(mdz_image_info, rgb_data),    (int64_t)offsetof(mdz_image_info, j_pre),
+        (int64_t)offsetof(mdz_image_info, drawing_area), (int64_t)offsetof(mdz_image_info, rnd_pal),
+        (int64_t)offsetof(mdz_image_info, real_width),  (int64_t)offsetof(mdz_image_info, real_height),
+        (int64_t)offsetof(mdz_image_info, user_width),  (int64_t)offsetof(mdz_image_info, user_height),
+        (int64_t)offsetof(mdz_image_info, aspect),      (int64_t)offsetof(mdz_image_info, aa_factor),
+        (int64_t)offsetof(mdz_image_info, family),      (int64_t)offsetof(mdz_image_info, fractal),
+        (int64_t)offsetof(mdz_image_info, colour_scale), (int64_t)offsetof(mdz_image_info, u.julia.c_re),
+        (int64_t)offsetof(mdz_image_info, u.julia.c_im), (int64_t)offsetof(mdz_image_info, palette_ip),
+        (int64_t)offsetof(mdz_image_info, zoom_new_win), (int64_t)offsetof(mdz_image_info, use_multi_prec),
+        (int64_t)offsetof(mdz_image_info, use_rounding), (int64_t)offsetof(mdz_image_info, precision),
+        (int64_t)offsetof(mdz_image_info, multi_prec_init_done), (int64_t)offsetof(mdz_image_info, rth_ptr),
+        (int64_t)offsetof(mdz_image_info, lines_drawn), (int64_t)offsetof(mdz_image_info, ui_ref_center),
+        (int64_t)sizeof(mdz_image_info),
+        (int64_t)offsetof(mdz_rthdata, img),            (int64_t)offsetof(mdz_rthdata, lines_drawn),
+        (int64_t)offsetof(mdz_rthdata, min_line_drawn), (int64_t)offsetof(mdz_rthdata, line_draw_count),
+        (int64_t)offsetof(mdz_rthdata, thread_count),   (int64_t)offsetof(mdz_rthdata, check_stop_px),
+        (int64_t)offsetof(mdz_rthdata, data),           (int64_t)sizeof(mdz_rthdata),
+    };
+    const int cnt = (int)(sizeof offs / sizeof offs[0]);
+    int k = 0;
+    for (; k < cnt && k < n; ++k)
+        out[k] = offs[k];
+    return k;
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+// Internal declarations shared by the libmdzgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "../../include/mdzgpu.h"
+
+namespace mdz {
+
+// Records the calling thread's last error (read by mdzgpu_last_error) and
+// prints it to stderr, MDZ's error channel (src/render_threads.c:179).
+void set_error(const char* fmt, ...);
+
+#define MDZ_CUDA_TRY(expr)                                                     \
+    do {                                                                       \
+        cudaError_t _e = (expr);                                               \
+        if (_e != cudaSuccess) {                                               \
+            ::mdz::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr,       \
+                             cudaGetErrorString(_e));                          \
+            return MDZGPU_ERR_CUDA;                                            \
+        }                                                                      \
+    } while (0)
+
+// Grows a device allocation to at least `bytes`; never shrinks.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t want);
+    void release();
+};
+
+// Grows a pinned, device-mapped host allocation.
+struct PinnedBuf {
+    void* host = nullptr;
+    void* dev = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t want);
+    void release();
+};
+
+// Per-frame device scratch for the work-queue kernels: tile counter,
+// pixel-iteration sum and per-tile-row completion counters.
+struct FrameSync {
+    unsigned int tile_counter;
+    unsigned int pad;
+    unsigned long long iter_sum;
+};
+
+}  // namespace mdz
+
+struct mdzgpu_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    mdz::DevBuf counts;     // int32 counts
+    mdz::DevBuf sync;       // FrameSync + tile-row counters
+    mdz::DevBuf coords;     // fixed-point pixel coordinates (MP path)
+    mdz::DevBuf orbit;      // reference orbit (perturbation)
+    mdz::DevBuf orbit_fx;   // fixed-point reference state
+    mdz::DevBuf aux;        // per-pixel float output (perturbation)
+    mdz::PinnedBuf pinned;  // small host-mapped status words
+    mdz::PinnedBuf staging; // pinned host copy of counts
+};
+
+namespace mdz {
+
+struct Fp64Launch {
+    int W, H;           // real frame size
+    int row0, nrows;    // rows rendered by this launch
+    int family, fractal;
+    uint32_t depth;
+    double xmin, xmax, ymax, jre, jim;
+    int32_t* out;       // out[(line - row0) * W + ix]
+    FrameSync* sync;
+    unsigned int* tile_rows_done;  // per 4-row band
+    volatile int* band_flags;      // host-mapped, per 4-row band (may be null)
+    volatile int* stop;            // host-mapped stop word (may be null)
+};
+int launch_fp64(mdzgpu_ctx* ctx, const Fp64Launch& p, cudaStream_t s);
+
+struct MpLaunch {
+    int W, H, row0, nrows;
+    int family, fractal;
+    uint32_t depth;
+    int words;               // 32-bit words per fixed-point number
+    const uint32_t* xs;      // [W][words] pixel x coordinates
+    const uint32_t* ys;      // [nrows][words] pixel y coordinates
+    const uint32_t* julia;   // [2][words] c_re, c_im (julia family)
+    int32_t* out;
+    FrameSync* sync;
+    unsigned int* tile_rows_done;
+    volatile int* band_flags;
+    volatile int* stop;
+};
+int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
+bool mp_words_supported(int words);
+// Word counts the multi-limb kernel is compiled for (one translation unit
+// each; the build reads this list).
+#define MDZ_MP_WORDS_LIST(X) X(4) X(6) X(8) X(10) X(12) X(16) X(20) X(24) X(28) X(34) X(36)
+template <int N>
+int launch_words(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
+
+struct OrbitLaunch {
+    int limbs;              // L radix-2^28 signed digits, F = 28 (L - 1)
+    const int* c_re;        // [L] centre, balanced signed digits
+    const int* c_im;
+    float2* zf;             // [max_k + 1] Z_k in FP32
+    double2* zd;            // [max_k + 1] Z_k mantissas in FP64 ...
+    int* ze;                // ... times 2^ze[k]
+    int max_k;              // last index computed (depth + 1)
+    int* out_len;           // number of valid entries (device)
+};
+int launch_orbit(const OrbitLaunch& p, cudaStream_t s);
+int orbit_max_limbs();
+
+struct PerturbLaunch {
+    int W, H, row0, nrows;
+    uint32_t depth;
+    double hs_m;            // half pixel spacing = hs_m * 2^hs_e, <= 40 bits
+    int hs_e;
+    const float2* zf;
+    const double2* zd;
+    const int* ze;
+    const int* orbit_len;   // device: valid orbit entries
+    int32_t* out;
+    float* mag;             // |z|^2 at escape (may be null)
+    FrameSync* sync;
+    unsigned long long* rebases;
+    volatile int* stop;
+};
+int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s);
+
+// Fixed-point conversion helpers (host).  A fixed-point number has `words`
+// 32-bit words, two's complement, least significant first, and
+// F = 32*words - 8 fractional bits.
+int fx_from_mpval(const mdzgpu_mpval* v, int words, uint32_t* out);
+int fx_from_mpfr(const mdz_mpfr* v, int words, uint32_t* out);
+int fx_from_mpf(const mdz_mpf* v, int words, uint32_t* out);
+double fx_to_double(const uint32_t* x, int words);
+// out = a + sign * (k * step) / div   (k, div > 0), truncated toward -inf
+void fx_affine(const uint32_t* a, const uint32_t* step, long k, long div,
+               int sign, int words, uint32_t* out);
+double mpfr_to_double_rn(const mdz_mpfr* v);
+bool fx_fits_coordinate(const uint32_t* x, int words);
+// Balanced radix-2^28 digits (L of them, F = 28 (L - 1)) of an mpval.
+int digits28_from_mpval(const mdzgpu_mpval* v, int L, int* out);
+// Half pixel spacing width / (2 W) rounded to 40 significant bits.
+int half_spacing(const mdzgpu_mpval* width, int W, double* hs_m, int* hs_e);
+int mp_words_for_precision(long precision);
+// Multi-limb render from fixed-point inputs (used by the drop-in layer).
+int mp_render_fixed(mdzgpu_ctx* ctx, const mdzgpu_frame* f, int words, const uint32_t* fxmin,
+                    const uint32_t* fymax, const uint32_t* fwidth, const uint32_t* fjre,
+                    const uint32_t* fjim, int32_t* d_out, int32_t* h_out, mdzgpu_stats* st,
+                    double t0);
+
+}  // namespace mdz

@@ -1,0 +1,227 @@
+// Multi-limb fixed-point escape-time kernel: the GPU form of MDZ's
+// multiprecision path.
+//
+// Reference loops (per iteration, same operation order):
+//   Mandelbrot          src/frac_mandel.c:25-52        (MPFR)  :55-82  (GMP)
+//   burning ship        src/frac_burning_ship.c:27-55  (MPFR)  :58-86  (GMP)
+//   generalized celtic  src/frac_generalized_celtic.c:27-55    :58-86
+//   hybrid              src/frac_variant.c:26-55               :58-87
+//   pixel -> coordinate src/fractal.c:159-192 (MPFR), :299-332 (GMP)
+// MPFR/GMP floats are replaced by N-word fixed point (fixed_point.cuh) with
+// at least precision+8 bits; counts agree with MPFR at the same precision
+// wherever MPFR at twice the precision agrees with it.
+//
+// One thread iterates one pixel; magnitudes and sign masks are kept
+// separately so the three products per iteration run on magnitudes.  c stays
+// in registers up to 16 words and moves to shared memory above that so the
+// 34/36-word (1088-bit class) kernels fit in registers.  Work is pulled in
+// 8x4 tiles per warp from an atomic counter, as in the FP64 kernel.
+#include "fixed_point.cuh"
+#include "internal.h"
+
+namespace mdz {
+namespace {
+
+constexpr int kTileW = 8;
+constexpr int kTileH = 4;
+
+template <int N>
+struct CRegs {
+    uint32_t w[N];
+    __device__ __forceinline__ uint32_t operator()(int k) const { return w[k]; }
+};
+
+template <int N>
+struct CShared {
+    const uint32_t* base;  // word k of this thread at base[k * stride]
+    int stride;
+    __device__ __forceinline__ uint32_t operator()(int k) const { return base[k * stride]; }
+};
+
+template <int N, int FRACTAL, class CG>
+__device__ __forceinline__ uint32_t escape_mp(uint32_t (&wre)[N], uint32_t (&wim)[N],
+                                              const CG& c_re, const CG& c_im, uint32_t depth)
+{
+    uint32_t wre2[N], wim2[N], acc[N + 2], t[N], d[N];
+    uint32_t sre = fx::abs_inplace<N>(wre);
+    uint32_t sim = fx::abs_inplace<N>(wim);
+    fx::sqr_trunc<N>(wre, acc);
+    fx::extract<N, 24>(acc, wre2);
+    fx::sqr_trunc<N>(wim, acc);
+    fx::extract<N, 24>(acc, wim2);
+    for (uint32_t wz = 1; wz <= depth; ++wz) {
+        // wim = 2.0 * wre * wim + c_im   (burning ship: 2 |wre wim| + c_im)
+        fx::mul_trunc<N>(wre, wim, acc);
+        fx::extract<N, 23>(acc, t);
+        const uint32_t mt = (FRACTAL == MDZ_BURNING_SHIP) ? 0u : (sre ^ sim);
+        fx::add_signed<N>(c_im, t, mt, wim);
+        // wre = wre2 - wim2 + c_re       (celtic: |wre2 - wim2| + c_re)
+        fx::sub<N>(wre2, wim2, d);
+        uint32_t md = 0u;
+        if (FRACTAL == MDZ_GENERALIZED_CELTIC || (FRACTAL == MDZ_VARIANT && (wz & 1u)))
+            md = (uint32_t)((int32_t)d[N - 1] >> 31);
+        fx::add_signed<N>(c_re, d, md, wre);
+        if (fx::big<N>(wre) || fx::big<N>(wim))
+            return wz;
+        sre = fx::abs_inplace<N>(wre);
+        sim = fx::abs_inplace<N>(wim);
+        // wim2 = wim * wim; wre2 = wre * wre
+        fx::sqr_trunc<N>(wim, acc);
+        fx::extract<N, 24>(acc, wim2);
+        fx::sqr_trunc<N>(wre, acc);
+        fx::extract<N, 24>(acc, wre2);
+        if (fx::sum_gt4<N>(wim2, wre2))
+            return wz;
+    }
+    return 0;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int N>
+__host__ __device__ constexpr bool c_in_smem()
+{
+    return N > 16;
+}
+
+template <int N>
+__host__ __device__ constexpr int block_threads()
+{
+    return N > 16 ? 128 : 256;
+}
+
+template <int N, int FRACTAL, bool JULIA>
+__global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p)
+{
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31;
+    const int tiles_x = (p.W + kTileW - 1) / kTileW;
+    const int tiles_y = (p.nrows + kTileH - 1) / kTileH;
+    const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y;
+    for (;;) {
+        unsigned tile = 0;
+        if (lane == 0)
+            tile = (p.stop && *p.stop) ? total : atomicAdd(&p.sync->tile_counter, 1u);
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        if (tile >= total)
+            break;
+        const int ty = (int)(tile / (unsigned)tiles_x);
+        const int tx = (int)(tile - (unsigned)ty * (unsigned)tiles_x);
+        const int ix = tx * kTileW + (lane & (kTileW - 1));
+        const int lrow = ty * kTileH + (lane / kTileW);
+        unsigned long long its = 0;
+        if (ix < p.W && lrow < p.nrows) {
+            uint32_t wre[N], wim[N];
+            const uint32_t* xs = p.xs + (size_t)ix * N;
+            const uint32_t* ys = p.ys + (size_t)lrow * N;
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                wre[k] = xs[k];
+                wim[k] = ys[k];
+            }
+            uint32_t n;
+            if constexpr (c_in_smem<N>()) {
+                const int stride = blockDim.x;
+                uint32_t* cre = smem + threadIdx.x;
+                uint32_t* cim = smem + (size_t)N * stride + threadIdx.x;
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+                    cre[k * stride] = JULIA ? p.julia[k] : wre[k];
+                    cim[k * stride] = JULIA ? p.julia[N + k] : wim[k];
+                }
+                CShared<N> gr{cre, stride}, gi{cim, stride};
+                n = escape_mp<N, FRACTAL>(wre, wim, gr, gi, p.depth);
+            } else {
+                CRegs<N> gr, gi;
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+                    gr.w[k] = JULIA ? p.julia[k] : wre[k];
+                    gi.w[k] = JULIA ? p.julia[N + k] : wim[k];
+                }
+                n = escape_mp<N, FRACTAL>(wre, wim, gr, gi, p.depth);
+            }
+            p.out[(size_t)lrow * p.W + ix] = (int32_t)n;
+            its = n ? n : p.depth;
+        }
+        its = warp_sum_u64(its);
+        if (p.band_flags)
+            __threadfence_system();
+        __syncwarp();
+        if (lane == 0) {
+            atomicAdd(&p.sync->iter_sum, its);
+            if (p.tile_rows_done) {
+                const unsigned done = atomicAdd(&p.tile_rows_done[ty], 1u) + 1u;
+                if (done == (unsigned)tiles_x && p.band_flags) {
+                    __threadfence_system();
+                    p.band_flags[ty] = 1;
+                }
+            }
+        }
+    }
+}
+
+template <int N, int FRACTAL, bool JULIA>
+int launch_typed(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
+{
+    constexpr int threads = block_threads<N>();
+    const size_t smem = c_in_smem<N>() ? (size_t)2 * N * threads * sizeof(uint32_t) : 0;
+    static int blocks_per_sm = 0;
+    if (!blocks_per_sm) {
+        if (smem > 48 * 1024)
+            MDZ_CUDA_TRY(cudaFuncSetAttribute(mp_frame_kernel<N, FRACTAL, JULIA>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &blocks_per_sm, mp_frame_kernel<N, FRACTAL, JULIA>, threads, smem));
+        if (blocks_per_sm < 1)
+            blocks_per_sm = 1;
+    }
+    const long tiles = (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
+    long grid = (long)ctx->num_sms * blocks_per_sm;
+    const long blocks_needed = (tiles + threads / 32 - 1) / (threads / 32);
+    if (grid > blocks_needed)
+        grid = blocks_needed;
+    if (grid < 1)
+        grid = 1;
+    mp_frame_kernel<N, FRACTAL, JULIA><<<(unsigned)grid, threads, smem, s>>>(p);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
+}  // namespace
+
+template <int N>
+int launch_words(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
+{
+    const bool julia = p.family == MDZ_FAMILY_JULIA;
+    switch (p.fractal) {
+    case MDZ_BURNING_SHIP:
+        return julia ? launch_typed<N, MDZ_BURNING_SHIP, true>(ctx, p, s)
+                     : launch_typed<N, MDZ_BURNING_SHIP, false>(ctx, p, s);
+    case MDZ_GENERALIZED_CELTIC:
+        return julia ? launch_typed<N, MDZ_GENERALIZED_CELTIC, true>(ctx, p, s)
+                     : launch_typed<N, MDZ_GENERALIZED_CELTIC, false>(ctx, p, s);
+    case MDZ_VARIANT:
+        return julia ? launch_typed<N, MDZ_VARIANT, true>(ctx, p, s)
+                     : launch_typed<N, MDZ_VARIANT, false>(ctx, p, s);
+    default:
+        return julia ? launch_typed<N, MDZ_MANDELBROT, true>(ctx, p, s)
+                     : launch_typed<N, MDZ_MANDELBROT, false>(ctx, p, s);
+    }
+}
+
+
+#ifdef MDZ_MP_WORDS
+// One translation unit per word count (the build compiles this file once for
+// every count in the list) keeps the large unrolled kernels compiling in
+// parallel.
+template int launch_words<MDZ_MP_WORDS>(mdzgpu_ctx*, const MpLaunch&, cudaStream_t);
+#endif
+
+}  // namespace mdz

@@ -1,0 +1,440 @@
+// Perturbation method for deep zooms (Mandelbrot family).
+//
+// The reference has no perturbation path: its only deep-zoom method is the
+// per-pixel MPFR loop (src/frac_mandel.c:25-52) at img->precision bits.  This
+// file is the new method named for the 2^-1000 workload:
+//
+// 1. Reference orbit.  One orbit Z_{k+1} = Z_k^2 + C (Z_0 = 0, Z_1 = C) of the
+//    frame centre is iterated exactly in multi-limb fixed point by ONE warp.
+//    Numbers are L signed radix-2^28 digits (value = sum d_i 2^(28 i - F),
+//    F = 28 (L-1) fractional bits), so every 28x28-bit partial product fits an
+//    IMAD.WIDE into a 64-bit column sum with no carry chain; the 2L product
+//    columns of Re and Im are spread over the 32 lanes and carries are
+//    resolved with three warp-shuffle passes.  Each Z_k is rounded to FP64
+//    (mantissa pair + int32 exponent, so tiny values near a nucleus keep full
+//    precision) and to FP32 for the pixel loop.
+//
+// 2. Pixels.  dz = z - Z_m is kept as an FP32 mantissa pair t with an int32
+//    exponent e (dz = t 2^e).  The hot step is plain FP32:
+//        t' = 2 Z_m t + 2^e t^2 + dc 2^-e
+//    with 2^e and dc 2^-e refreshed only when |t| leaves [2^-32, 2^32].
+//    FP64 is used only where precision is lost otherwise: the rebase test
+//    |Z_m + dz| < |dz| (screened in FP32: it can only hold when
+//    |dz| >= |Z_m| / 2), the rebase itself dz <- Z_m + dz, m <- 0 (Zhuoran's
+//    rebasing), and the full floatexp step needed when Z_m is tiny and dz is
+//    below the FP32 range.  Escape: |Z_m + dz|^2 > 4, evaluated in FP32.
+//
+// Counts follow MDZ's convention (src/frac_mandel.c:11-20): z starts at c,
+// the first update is iteration 1, the count is the first iteration whose
+// result has |z|^2 > 4, or 0 if none within depth.
+#include <math.h>
+
+#include "internal.h"
+
+namespace mdz {
+namespace {
+
+constexpr int kTileW = 8;
+constexpr int kTileH = 4;
+constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
+
+// --------------------------------------------------------------------------
+// Reference orbit
+// --------------------------------------------------------------------------
+
+__device__ __forceinline__ void digit_split(long long v, long long& digit, long long& carry)
+{
+    // signed digit in [-2^27, 2^27), v = digit + carry * 2^28
+    digit = ((v + (1ll << 27)) & ((1ll << 28) - 1)) - (1ll << 27);
+    carry = (v - digit) >> 28;
+}
+
+// value of 4 digits starting at `top` (inclusive, downwards) as a double
+// mantissa m and exponent x: value ~ m * 2^x, |m| in [0.5, 1) unless zero.
+__device__ void limbs_to_double(const int* d, int L, double& m, int& x)
+{
+    int top = L - 1;
+    while (top > 0 && d[top] == 0)
+        --top;
+    double v = (double)d[top];
+    if (top >= 1)
+        v += ldexp((double)d[top - 1], -28);
+    if (top >= 2)
+        v += ldexp((double)d[top - 2], -56);
+    if (top >= 3)
+        v += ldexp((double)d[top - 3], -84);
+    // v * 2^(28 top - F)
+    int ex = 0;
+    m = frexp(v, &ex);
+    x = ex + 28 * top - 28 * (L - 1);
+    if (v == 0.0) {
+        m = 0.0;
+        x = 0;
+    }
+}
+
+__global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
+{
+    __shared__ int zr[kMaxOrbitLimbs], zi[kMaxOrbitLimbs], cr[kMaxOrbitLimbs], ci[kMaxOrbitLimbs];
+    const int lane = threadIdx.x;
+    const int L = p.limbs;
+    for (int j = lane; j < L; j += 32) {
+        cr[j] = p.c_re[j];
+        ci[j] = p.c_im[j];
+        zr[j] = p.c_re[j];
+        zi[j] = p.c_im[j];
+    }
+    __syncwarp();
+    // Z_0 = 0, Z_1 = C
+    if (lane == 0) {
+        p.zf[0] = make_float2(0.f, 0.f);
+        p.zd[0] = make_double2(0.0, 0.0);
+        p.ze[0] = 0;
+    }
+    const int cbase = L - 4;       // lowest column computed (3 guard columns)
+    const int ctop = 2 * L - 2;    // highest column
+    int k = 1;
+    int escaped = 0;
+    for (;; ++k) {
+        // ---- store Z_k ----
+        double mr = 0.0, mi = 0.0;
+        int xr = 0, xi = 0;
+        if (lane == 0)
+            limbs_to_double(zr, L, mr, xr);
+        if (lane == 1)
+            limbs_to_double(zi, L, mi, xi);
+        mi = __shfl_sync(0xffffffffu, mi, 1);
+        xi = __shfl_sync(0xffffffffu, xi, 1);
+        if (lane == 0) {
+            // common exponent for the pair
+            const int xe = (mr == 0.0) ? xi : (mi == 0.0 ? xr : max(xr, xi));
+            const double dr = ldexp(mr, xr - xe);
+            const double di = ldexp(mi, xi - xe);
+            // store with exponent 0 whenever the plain double is normal
+            int store_e = 0;
+            double sr = ldexp(dr, xe), si = ldexp(di, xe);
+            if (xe < -960) {
+                store_e = xe;
+                sr = dr;
+                si = di;
+            }
+            p.zd[k] = make_double2(sr, si);
+            p.ze[k] = store_e;
+            p.zf[k] = make_float2((float)ldexp(dr, xe), (float)ldexp(di, xe));
+            const double vr = ldexp(dr, xe), vi = ldexp(di, xe);
+            escaped = (vr * vr + vi * vi > 4.0) ? 1 : 0;
+        }
+        escaped = __shfl_sync(0xffffffffu, escaped, 0);
+        if (escaped || k >= p.max_k)
+            break;
+        // ---- Z_{k+1} = Z_k^2 + C ----
+        long long vr[3], vi[3];
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            vr[s] = 0;
+            vi[s] = 0;
+            const int c = cbase + lane + 32 * s;
+            if (c > ctop)
+                continue;
+            const int ilo = c - (L - 1) > 0 ? c - (L - 1) : 0;
+            const int ihi = (c - 1) >> 1;  // i < j = c - i
+            long long pr = 0, pi = 0;
+            for (int i = ilo; i <= ihi; ++i) {
+                const int j = c - i;
+                const long long ari = zr[i], aii = zi[i], arj = zr[j], aij = zi[j];
+                pr += ari * arj - aii * aij;
+                pi += ari * aij + arj * aii;
+            }
+            long long dr = 0, di = 0;
+            if (!(c & 1)) {
+                const int h = c >> 1;
+                if (h <= L - 1) {
+                    const long long a = zr[h], b = zi[h];
+                    dr = a * a - b * b;
+                    di = a * b;
+                }
+            }
+            vr[s] = 2 * pr + dr;
+            vi[s] = 2 * (pi + di);
+            if (c >= L - 1) {
+                vr[s] += cr[c - (L - 1)];
+                vi[s] += ci[c - (L - 1)];
+            }
+        }
+        // ---- carry propagation: three passes, column c+1 is lane+1 (slot
+        // s) or lane 0 of slot s+1 ----
+#pragma unroll
+        for (int pass = 0; pass < 3; ++pass) {
+            long long dgr[3], dgi[3], cyr[3], cyi[3];
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                digit_split(vr[s], dgr[s], cyr[s]);
+                digit_split(vi[s], dgi[s], cyi[s]);
+            }
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                long long inr = __shfl_up_sync(0xffffffffu, cyr[s], 1);
+                long long ini = __shfl_up_sync(0xffffffffu, cyi[s], 1);
+                const long long wrapr = __shfl_sync(0xffffffffu, s > 0 ? cyr[s - 1] : 0ll, 31);
+                const long long wrapi = __shfl_sync(0xffffffffu, s > 0 ? cyi[s - 1] : 0ll, 31);
+                if (lane == 0) {
+                    inr = wrapr;
+                    ini = wrapi;
+                }
+                vr[s] = dgr[s] + inr;
+                vi[s] = dgi[s] + ini;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            const int c = cbase + lane + 32 * s;
+            if (c <= ctop && c >= L - 1) {
+                zr[c - (L - 1)] = (int)vr[s];
+                zi[c - (L - 1)] = (int)vi[s];
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0)
+        *p.out_len = k + 1;  // entries 0..k are valid
+}
+
+// --------------------------------------------------------------------------
+// Pixels
+// --------------------------------------------------------------------------
+
+struct PixState {
+    float tr, ti;   // dz mantissas
+    int e;          // dz = t * 2^e
+    float s;        // 2^e (0 below the FP32 range)
+    float s2x4;     // 4 * 2^(2e), 0 when e < -63
+    float dcr, dci; // dc * 2^-e
+    bool slow_if_tiny;
+    bool force_slow;
+};
+
+__device__ __forceinline__ void refresh_scale(PixState& st, float dcm_r, float dcm_i, int dce)
+{
+    st.s = ldexpf(1.0f, st.e);
+    st.s2x4 = st.e >= -63 ? 4.0f * st.s * st.s : 0.0f;
+    st.dcr = ldexpf(dcm_r, dce - st.e);
+    st.dci = ldexpf(dcm_i, dce - st.e);
+    st.slow_if_tiny = st.e < -120;
+    // dc * 2^-e would overflow FP32 (dz far below dc); a pixel with dc == 0
+    // is the reference point itself and never needs it.
+    st.force_slow = (dcm_r != 0.f || dcm_i != 0.f) && (dce - st.e) > 120;
+}
+
+// Set t, e from a double pair scaled by 2^E.
+__device__ __forceinline__ void set_from_double(PixState& st, double xr, double xi, int E)
+{
+    const double a = fmax(fabs(xr), fabs(xi));
+    if (a == 0.0) {
+        st.tr = 0.f;
+        st.ti = 0.f;
+        st.e = E;
+        return;
+    }
+    const int k = ilogb(a);
+    st.tr = (float)ldexp(xr, -k);
+    st.ti = (float)ldexp(xi, -k);
+    st.e = E + k;
+}
+
+__device__ __forceinline__ int dexp_of(double x)
+{
+    return x == 0.0 ? -100000 : ilogb(x);
+}
+
+template <bool WANT_MAG>
+__device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
+                                  float& mag_out, unsigned& rebases)
+{
+    const float dcf_r = (float)dcm_r, dcf_i = (float)dcm_i;
+    PixState st;
+    set_from_double(st, dcm_r, dcm_i, dce);
+    refresh_scale(st, dcf_r, dcf_i, dce);
+    int m = 1;
+    const int K = *p.orbit_len;  // entries 0..K-1 valid
+    float2 Z = p.zf[1];
+    float mag = 0.f;
+    for (uint32_t wz = 1; wz <= p.depth; ++wz) {
+        if (m >= K - 1) {
+            // end of the reference orbit: rebase onto Z_0 = 0
+            const double2 zd = p.zd[m];
+            const int ze = p.ze[m];
+            const int E = max(dexp_of(fmax(fabs(zd.x), fabs(zd.y))) + ze, st.e + 40);
+            const double zr = ldexp(zd.x, ze - E) + ldexp((double)st.tr, st.e - E);
+            const double zi = ldexp(zd.y, ze - E) + ldexp((double)st.ti, st.e - E);
+            set_from_double(st, zr, zi, E);
+            refresh_scale(st, dcf_r, dcf_i, dce);
+            m = 0;
+            Z = p.zf[0];
+            ++rebases;
+        }
+        const float zm2 = Z.x * Z.x + Z.y * Z.y;
+        if (st.force_slow || (st.slow_if_tiny && zm2 < 7.5e-37f /* 2^-120 */)) {
+            // full floatexp step in FP64: dz' = 2 Z dz + dz^2 + dc
+            const double2 zd = p.zd[m];
+            const int ze = p.ze[m];
+            const double tr = st.tr, ti = st.ti;
+            // A = 2 Z t  * 2^(ze + e)
+            const double ar = 2.0 * (zd.x * tr - zd.y * ti), ai = 2.0 * (zd.x * ti + zd.y * tr);
+            const int ae = ze + st.e;
+            // B = t^2 * 2^(2e)
+            const double br = tr * tr - ti * ti, bi = 2.0 * tr * ti;
+            const int be = 2 * st.e;
+            const int E = max(max(dexp_of(fmax(fabs(ar), fabs(ai))) + ae,
+                                  dexp_of(fmax(fabs(br), fabs(bi))) + be),
+                              dexp_of(fmax(fabs(dcm_r), fabs(dcm_i))) + dce);
+            const double rr = ldexp(ar, ae - E) + ldexp(br, be - E) + ldexp(dcm_r, dce - E);
+            const double ri = ldexp(ai, ae - E) + ldexp(bi, be - E) + ldexp(dcm_i, dce - E);
+            set_from_double(st, rr, ri, E);
+            refresh_scale(st, dcf_r, dcf_i, dce);
+        } else {
+            const float tr = st.tr, ti = st.ti;
+            const float u = tr + tr, v = ti + ti;
+            const float a = fmaf(tr, tr, -ti * ti);  // t^2 real
+            const float b = tr * v;                  // t^2 imag
+            st.tr = fmaf(Z.x, u, fmaf(-Z.y, v, fmaf(st.s, a, st.dcr)));
+            st.ti = fmaf(Z.x, v, fmaf(Z.y, u, fmaf(st.s, b, st.dci)));
+        }
+        ++m;
+        Z = p.zf[m];
+        const float zr = fmaf(st.s, st.tr, Z.x);
+        const float zi = fmaf(st.s, st.ti, Z.y);
+        mag = fmaf(zr, zr, zi * zi);
+        if (mag > 4.0f) {
+            mag_out = mag;
+            return wz;
+        }
+        const float dd = fmaf(st.tr, st.tr, st.ti * st.ti);
+        const float zn2 = fmaf(Z.x, Z.x, Z.y * Z.y);
+        const bool maybe = st.e >= -63 ? (st.s2x4 * dd >= zn2) : (zn2 < 8.7e-19f /* 2^-60 */);
+        if (maybe) {
+            // rebase test |Z_m + dz| < |dz| in FP64
+            const double2 zd = p.zd[m];
+            const int ze = p.ze[m];
+            const int E = max(dexp_of(fmax(fabs(zd.x), fabs(zd.y))) + ze, st.e + 40);
+            const double dr = ldexp((double)st.tr, st.e - E), di = ldexp((double)st.ti, st.e - E);
+            const double fr = ldexp(zd.x, ze - E) + dr, fi = ldexp(zd.y, ze - E) + di;
+            if (fr * fr + fi * fi < dr * dr + di * di) {
+                set_from_double(st, fr, fi, E);
+                refresh_scale(st, dcf_r, dcf_i, dce);
+                m = 0;
+                Z = p.zf[0];
+                ++rebases;
+                continue;
+            }
+        }
+        const float amax = fmaxf(fabsf(st.tr), fabsf(st.ti));
+        if ((amax > 4.2949673e9f || amax < 2.3283064e-10f) && amax != 0.0f) {
+            const int k = ((__float_as_int(amax) >> 23) & 0xff) - 127;
+            const float sc = ldexpf(1.0f, -k);
+            st.tr *= sc;
+            st.ti *= sc;
+            st.e += k;
+            refresh_scale(st, dcf_r, dcf_i, dce);
+        }
+    }
+    mag_out = mag;
+    return 0;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <bool WANT_MAG>
+__global__ void __launch_bounds__(256) perturb_frame_kernel(PerturbLaunch p)
+{
+    const int lane = threadIdx.x & 31;
+    const int tiles_x = (p.W + kTileW - 1) / kTileW;
+    const int tiles_y = (p.nrows + kTileH - 1) / kTileH;
+    const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y;
+    for (;;) {
+        unsigned tile = 0;
+        if (lane == 0)
+            tile = (p.stop && *p.stop) ? total : atomicAdd(&p.sync->tile_counter, 1u);
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        if (tile >= total)
+            break;
+        const int ty = (int)(tile / (unsigned)tiles_x);
+        const int tx = (int)(tile - (unsigned)ty * (unsigned)tiles_x);
+        const int ix = tx * kTileW + (lane & (kTileW - 1));
+        const int lrow = ty * kTileH + (lane / kTileW);
+        unsigned long long its = 0;
+        unsigned reb = 0;
+        if (ix < p.W && lrow < p.nrows) {
+            const int line = p.row0 + lrow;
+            // dc = ((2 ix - W) hs, (H - 2 line) hs), hs = half pixel spacing
+            const double dcm_r = (double)(2 * ix - p.W) * p.hs_m;
+            const double dcm_i = (double)(p.H - 2 * line) * p.hs_m;
+            float mag = 0.f;
+            const uint32_t n = perturb_pixel<WANT_MAG>(p, dcm_r, dcm_i, p.hs_e, mag, reb);
+            const size_t o = (size_t)lrow * p.W + ix;
+            p.out[o] = (int32_t)n;
+            if (WANT_MAG)
+                p.mag[o] = mag;
+            its = n ? n : p.depth;
+        }
+        its = warp_sum_u64(its);
+        unsigned long long rb = warp_sum_u64((unsigned long long)reb);
+        __syncwarp();
+        if (lane == 0) {
+            atomicAdd(&p.sync->iter_sum, its);
+            if (rb)
+                atomicAdd(p.rebases, rb);
+        }
+    }
+}
+
+}  // namespace
+
+int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
+{
+    if (p.limbs < 5 || p.limbs > kMaxOrbitLimbs) {
+        set_error("orbit: %d limbs outside [5, %d]", p.limbs, kMaxOrbitLimbs);
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    orbit_kernel<<<1, 32, 0, s>>>(p);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
+int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s)
+{
+    static int bps[2] = {0, 0};
+    const int w = p.mag ? 1 : 0;
+    if (!bps[w]) {
+        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &bps[w], w ? perturb_frame_kernel<true> : perturb_frame_kernel<false>, 256, 0));
+        if (bps[w] < 1)
+            bps[w] = 1;
+    }
+    const long tiles = (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
+    long grid = (long)ctx->num_sms * bps[w];
+    const long blocks_needed = (tiles + 7) / 8;
+    if (grid > blocks_needed)
+        grid = blocks_needed;
+    if (grid < 1)
+        grid = 1;
+    if (w)
+        perturb_frame_kernel<true><<<(unsigned)grid, 256, 0, s>>>(p);
+    else
+        perturb_frame_kernel<false><<<(unsigned)grid, 256, 0, s>>>(p);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
+int orbit_max_limbs()
+{
+    return kMaxOrbitLimbs;
+}
+
+}  // namespace mdz

@@ -1,0 +1,418 @@
+"""Generates the committed golden fixtures and seeded views (run here, where
+the reference sources exist; the GPU machine only reads the outputs).
+
+  python tests/golden/make_golden.py fp64      # fp64_*.npz  (reference double build)
+  python tests/golden/make_golden.py views     # views.json  (seeded ray bisection)
+  python tests/golden/make_golden.py mp        # mp_*.npz    (reference MPFR path, p and 2p)
+  python tests/golden/make_golden.py perturb   # perturb_c4.npz (MPFR at 2176 bits)
+  python tests/golden/make_golden.py abi       # abi_layout.json (reference struct offsets)
+
+Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
+(oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
+own rth_* thread pool, or, for explicit pixel lists, from its frac_*_mpfr
+loop through the oracle restatement (checked identical to the reference on
+every fixture here).  Seeds: numpy PCG64 with the seeds written below.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import math
+import sys
+import time
+from fractions import Fraction
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from mdz_gb300.mpval import MpVal, hexfloat  # noqa: E402
+from mdz_gb300.views import View  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+GOLD = Path(__file__).resolve().parent
+THREADS = 8
+JULIA_C = ("-0.8", "0.156")
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, np.int32).tobytes()).hexdigest()
+
+
+def pixel_iters(a: np.ndarray, depth: int) -> int:
+    a = a.astype(np.int64)
+    return int(np.where(a == 0, depth, a).sum())
+
+
+# --------------------------------------------------------------------------
+# FP64 fixtures
+# --------------------------------------------------------------------------
+
+def fp64_views() -> list[View]:
+    vs = [View("c1", 240, 180, 1000, "-0.75", "0", "3.0")]
+    # every formula x family on small frames
+    centres = {0: ("-0.75", "0.1", "3.0"), 1: ("-0.45", "-0.5", "3.4"),
+               2: ("-0.5", "0.2", "3.2"), 3: ("-0.6", "0.15", "3.2")}
+    for fr, (cx, cy, sz) in centres.items():
+        vs.append(View(f"f{fr}_mandel", 96, 64, 600, cx, cy, sz, fractal=fr))
+        vs.append(View(f"f{fr}_julia", 96, 64, 600, "0", "0", "3.2", fractal=fr, family=1,
+                       julia_re=JULIA_C[0], julia_im=JULIA_C[1]))
+    # anti-aliased, odd sizes, a zoomed view with deep counts, depth 1
+    vs.append(View("aa3", 40, 30, 800, "-0.7436447860", "0.1318252536", "0.00003", aa=3))
+    vs.append(View("odd", 37, 23, 300, "-0.5", "0", "3.5"))
+    vs.append(View("depth1", 33, 17, 1, "-0.5", "0", "4.0"))
+    vs.append(View("deep", 128, 96, 20000, "-0.74364478", "0.13182525", "1e-6"))
+    return vs
+
+
+def make_fp64() -> None:
+    out = {}
+    for v in fp64_views():
+        t0 = time.time()
+        ref, _ = O.ref_render(v, threads=THREADS, variant="d")
+        ld, _ = O.ref_render(v, threads=THREADS, variant="ld")
+        r = v.rect()
+        xmin, xmax, ymax = r.doubles()
+        jre = float(v.julia()[0].to_fraction()) if v.family else 0.0
+        jim = float(v.julia()[1].to_fraction()) if v.family else 0.0
+        mine, _ = O.render_fp64(v.real_width, v.real_height, v.depth, xmin, xmax, ymax,
+                                v.family, v.fractal, (jre, jim), aa=v.aa, threads=THREADS)
+        assert np.array_equal(ref, mine), f"oracle restatement differs from reference on {v.name}"
+        out[v.name] = ref
+        print(f"{v.name}: {ref.shape} iters={pixel_iters(ref, v.depth)} "
+              f"ld-differs={int((ld != ref).sum())} ({time.time() - t0:.1f}s)")
+    meta = {v.name: dict(v.__dict__, rect=[hexfloat(Fraction(x)) for x in v.rect().doubles()],
+                         sha256=sha(out[v.name]), pixel_iters=pixel_iters(out[v.name], v.depth))
+            for v in fp64_views()}
+    np.savez_compressed(GOLD / "fp64_counts.npz", **out)
+    (GOLD / "fp64_views.json").write_text(json.dumps(meta, indent=1, default=str))
+
+
+# --------------------------------------------------------------------------
+# Seeded views (ray bisection on the reference's own escape loops)
+# --------------------------------------------------------------------------
+
+def ray_dir(seed: int) -> tuple[float, float]:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    theta = float(rng.uniform(0.0, 2.0 * math.pi))
+    return math.cos(theta), math.sin(theta)
+
+
+def bisect_fp64(seed: int, depth: int) -> tuple[float, float]:
+    """Ray from 0 at a seeded angle; bisect r in [0, 2] on 'count == 0 at
+    depth' (reference double loop) to 53-bit precision."""
+    ct, st = ray_dir(seed)
+    lo, hi = 0.0, 2.0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if mid == lo or mid == hi:
+            break
+        if O.lib().mdzo_point_fp64(0, depth, mid * ct, mid * st) == 0:
+            lo = mid
+        else:
+            hi = mid
+    return lo * ct, lo * st
+
+
+def bisect_mpfr(seed: int, depth: int, prec: int, start_bits: int = 50) -> tuple[Fraction, Fraction]:
+    """The same ray bisection continued in MPFR at `prec` bits; 7 points per
+    round on THREADS cores (an 8-ary search, 3 bits per round)."""
+    ct, st = (Fraction(x) for x in ray_dir(seed))
+    lo, hi = Fraction(0), Fraction(2)
+    # coarse stage in FP64 (identical predicate where doubles suffice)
+    for _ in range(start_bits):
+        mid = (lo + hi) / 2
+        if O.lib().mdzo_point_fp64(0, depth, float(mid * ct), float(mid * st)) == 0:
+            lo = mid
+        else:
+            hi = mid
+    k = 8
+    while hi - lo > Fraction(2) ** (-prec):
+        pts = [lo + (hi - lo) * i / k for i in range(1, k)]
+        cre = [MpVal.from_fraction(p * ct, prec).hex() for p in pts]
+        cim = [MpVal.from_fraction(p * st, prec).hex() for p in pts]
+        counts, _ = O.points_mpfr(cre, cim, depth, prec, threads=THREADS)
+        inside = [c == 0 for c in counts]
+        # last inside point before the first outside one
+        new_lo, new_hi = lo, hi
+        for p, ins in zip(pts, inside):
+            if ins:
+                new_lo = p
+            else:
+                new_hi = p
+                break
+        lo, hi = new_lo, new_hi
+    c_re = MpVal.from_fraction(lo * ct, prec).to_fraction()
+    c_im = MpVal.from_fraction(lo * st, prec).to_fraction()
+    return c_re, c_im
+
+
+def make_views() -> None:
+    views = {}
+    # C1: fixed
+    views["c1"] = dict(name="c1", width=240, height=180, depth=1000, cx="-0.75", cy="0",
+                       size="3.0", precision=80, aa=1)
+    # C2: FP64, 1920x1080 x3 AA, maxiter 20000, width 1e-11, seed 2
+    t0 = time.time()
+    cx, cy = bisect_fp64(seed=2, depth=20000)
+    views["c2"] = dict(name="c2", width=1920, height=1080, depth=20000, cx=hexfloat(Fraction(cx)),
+                       cy=hexfloat(Fraction(cy)), size="1e-11", precision=80, aa=3, seed=2)
+    print("c2", cx, cy, f"{time.time() - t0:.1f}s")
+    # C3: 256-bit, 640x480, width 2^-200, maxiter 50000, seed 3, offset
+    t0 = time.time()
+    bre, bim = bisect_mpfr(seed=3, depth=50000, prec=256)
+    rng = np.random.Generator(np.random.PCG64(1003))
+    u1, u2 = (Fraction(float(x)) for x in rng.uniform(-0.5, 0.5, size=2))
+    w3 = Fraction(1, 2 ** 200)
+    views["c3"] = dict(name="c3", width=640, height=480, depth=50000,
+                       cx=hexfloat(MpVal.from_fraction(bre + u1 * w3, 256).to_fraction()),
+                       cy=hexfloat(MpVal.from_fraction(bim + u2 * w3, 256).to_fraction()),
+                       size=hexfloat(w3), precision=256, aa=1, multi_prec=True, rounding=True,
+                       seed=3)
+    print("c3", f"{time.time() - t0:.1f}s")
+    (GOLD / "views.json").write_text(json.dumps(views, indent=1))
+    # C4: perturbation, 1920x1080, width 2^-1000, 1088-bit centre, maxiter 200000, seed 4
+    t0 = time.time()
+    bre, bim = bisect_mpfr(seed=4, depth=200000, prec=1088)
+    views["c4"] = dict(name="c4", width=1920, height=1080, depth=200000, cx=hexfloat(bre),
+                       cy=hexfloat(bim), size=hexfloat(Fraction(1, 2 ** 1000)), precision=1088,
+                       aa=1, seed=4)
+    print("c4", f"{time.time() - t0:.1f}s")
+    (GOLD / "views.json").write_text(json.dumps(views, indent=1))
+
+
+# --------------------------------------------------------------------------
+# Multiprecision fixtures (reference MPFR path at p and 2p)
+# --------------------------------------------------------------------------
+
+def mdz_mpfr_c(v: View, prec: int, ix: int, line: int) -> tuple[Fraction, Fraction]:
+    """c of pixel (ix, line) exactly as fractal_mpfr_calculate_line computes
+    it at `prec` bits (src/fractal.c:159-186) from image_info's rect."""
+    from mdz_gb300.views import mdz_rect
+    r = mdz_rect(v.width, v.height, prec, v.cx, v.cy, v.size)
+
+    def rn(x):
+        return MpVal.from_fraction(x, prec).to_fraction()
+    W = v.real_width
+    width, xmin, ymax = r.width.to_fraction(), r.xmin.to_fraction(), r.ymax.to_fraction()
+    t1 = rn(rn(width / W) * line)
+    y = rn(ymax - t1)
+    x = rn(rn(rn(Fraction(ix, W)) * width) + xmin)
+    return x, y
+
+
+GALLERY = Path("/root/reference/gallery")
+
+
+def gallery_views(width: int = 64) -> list[View]:
+    """The reference's saved deep views (gallery/*.mdz), shrunk to `width`
+    pixels across; rect-form files are turned into centre/size exactly."""
+    from mdz_gb300.mpval import parse_number
+    vs = []
+    for f in sorted(GALLERY.glob("*.mdz")):
+        kv = {}
+        for line in f.read_text().splitlines():
+            parts = line.split(None, 1)
+            if len(parts) == 2 and parts[0] in (
+                    "fractal", "family", "depth", "aspect", "precision", "cx", "cy", "size",
+                    "xmin", "xmax", "ymax"):
+                kv.setdefault(parts[0], parts[1].strip())
+            if line.strip() == "palette":
+                break
+        aspect = float(kv.get("aspect", "1.3333333333333333"))
+        if "cx" in kv:
+            cx, cy, size = (parse_number(kv[k]) for k in ("cx", "cy", "size"))
+        else:
+            xmin, xmax, ymax = (parse_number(kv[k]) for k in ("xmin", "xmax", "ymax"))
+            size = xmax - xmin
+            cx = (xmin + xmax) / 2
+            cy = ymax - size / Fraction(aspect) / 2
+        if aspect < 1:
+            continue
+        prec = int(kv.get("precision", "80"))
+        H = max(8, int(round(width / aspect)))
+        frac = {"mandelbrot": 0, "burning ship": 1, "generalized celtic": 2,
+                "mandel-celtic hybrid": 3}[kv.get("fractal", "mandelbrot")]
+        if frac != 0 and "family" not in kv:
+            frac = 0
+        digits = prec // 3 + 10
+        vs.append(View(f"gal_{f.stem}", width, H, int(kv["depth"]), _dec(cx, digits),
+                       _dec(cy, digits), _dec(size, digits), precision=prec,
+                       multi_prec=True, rounding=True, fractal=frac))
+    return vs
+
+
+def _dec(x: Fraction, digits: int) -> str:
+    """Decimal string with `digits` significant digits (exact enough for
+    parsing at the view's precision)."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = digits
+    return str(Decimal(x.numerator) / Decimal(x.denominator))
+
+
+def mp_views() -> list[View]:
+    c3 = json.loads((GOLD / "views.json").read_text())["c3"]
+    vs = gallery_views()
+    for fr in range(4):
+        vs.append(View(f"mp128_f{fr}", 48, 32, 1500, c3["cx"], c3["cy"], "0x1p-60",
+                       precision=128, multi_prec=True, fractal=fr))
+    vs.append(View("mp256_c3zoom", 64, 48, 4000, c3["cx"], c3["cy"], "0x1p-180",
+                   precision=256, multi_prec=True))
+    for fr in (1, 2):
+        vs.append(View(f"mp96_shallow_f{fr}", 40, 30, 800, "-0.6", "0.3", "0.05",
+                       precision=96, multi_prec=True, fractal=fr))
+    vs.append(View("mp_julia", 40, 30, 1000, "0.01", "0.02", "0x1p-50", precision=128,
+                   multi_prec=True, family=1, julia_re="-0.8", julia_im="0.156"))
+    return vs
+
+
+def make_mp() -> None:
+    out, meta = {}, {}
+    for v in mp_views():
+        t0 = time.time()
+        ref, _ = O.ref_render(v, threads=THREADS)
+        v2 = View.from_dict(dict(v.__dict__, precision=2 * v.precision))
+        ref2, _ = O.ref_render(v2, threads=THREADS)
+        out[v.name] = ref
+        out[v.name + "__2p"] = ref2
+        meta[v.name] = dict(v.__dict__)
+        print(f"{v.name}: confirmed {(ref == ref2).mean():.4f} "
+              f"iters={pixel_iters(ref, v.depth)} ({time.time() - t0:.1f}s)")
+    # config 3 (640x480, 256 bits, width 2^-200, maxiter 50000) on a
+    # subsampled pixel grid: every 8th column and row, at p and 2p
+    c3 = View.from_dict(json.loads((GOLD / "views.json").read_text())["c3"])
+    step = 8
+    ixs = list(range(0, c3.real_width, step))
+    lns = list(range(0, c3.real_height, step))
+    for prec, key in ((c3.precision, "c3_sub"), (2 * c3.precision, "c3_sub__2p")):
+        t0 = time.time()
+        cre, cim = [], []
+        for ln in lns:
+            for ix in ixs:
+                x, y = mdz_mpfr_c(c3, prec, ix, ln)
+                cre.append(hexfloat(x))
+                cim.append(hexfloat(y))
+        counts, _ = O.points_mpfr(cre, cim, c3.depth, prec, threads=THREADS)
+        out[key] = counts.reshape(len(lns), len(ixs)).astype(np.int32)
+        print(f"{key}: {time.time() - t0:.1f}s")
+    meta["c3_sub"] = dict(c3.__dict__, step=step)
+    # the GMP callback: reference's own gxmin/gymax/gwidth (the values its
+    # mpfr_to_gmp string conversion leaves, src/my_mpfr_to_str.c:68)
+    g = View("gmp_small", 48, 32, 1200, "-0.7436447860", "0.1318252536", "0.00002",
+             precision=128, multi_prec=True, rounding=False)
+    out["gmp_small"], _ = O.ref_render(g, threads=THREADS)
+    d = O.ref_view_dump(g)
+    meta["gmp_small"] = dict(g.__dict__, gmp={k: d[k] for k in ("gxmin", "gymax", "gwidth")})
+    np.savez_compressed(GOLD / "mp_counts.npz", **out)
+    (GOLD / "mp_views.json").write_text(json.dumps(meta, indent=1, default=str))
+
+
+# --------------------------------------------------------------------------
+# Perturbation fixtures (MPFR at twice the centre precision)
+# --------------------------------------------------------------------------
+
+def perturb_c(cx: Fraction, cy: Fraction, width: Fraction, W: int, H: int, ix: int, line: int):
+    """Pixel c of the perturbation geometry: hs = width / (2 W) rounded to 40
+    significant bits (mdzgpu_perturb_spacing), c = centre + ((2 ix - W) hs,
+    (H - 2 line) hs)."""
+    q = width / (2 * W)
+    k = q.numerator.bit_length() - q.denominator.bit_length()
+    if Fraction(2) ** k > q:
+        k -= 1
+    m = q / Fraction(2) ** k                       # [1, 2)
+    m = Fraction(round(m * 2 ** 39), 2 ** 39)     # ties to even, 40 bits
+    hs = m * Fraction(2) ** k
+    return cx + (2 * ix - W) * hs, cy + (H - 2 * line) * hs
+
+
+def make_perturb() -> None:
+    views = json.loads((GOLD / "views.json").read_text())
+    out, meta = {}, {}
+    # small full frames: around the c3 / c4 centres, around the Misiurewicz
+    # point c = i (structure at every scale), and the gallery's Mandelbrot views
+    frames = [("p_c3_200", views["c3"]["cx"], views["c3"]["cy"], 64, 48, 6000,
+               Fraction(2) ** -200, 256),
+              ("p_c4_600", views["c4"]["cx"], views["c4"]["cy"], 48, 36, 8000,
+               Fraction(2) ** -600, 704)]
+    for wexp, depth in ((-200, 3000), (-600, 6000), (-1000, 8000)):
+        frames.append((f"p_mis_i_{-wexp}", "0", "1", 64, 48, depth, Fraction(2) ** wexp,
+                       -wexp + 64))
+    frames.append(("p_mis_b_1000", "-0.10109636384562", "0.95628651080914", 48, 36, 8000,
+                   Fraction(2) ** -1000, 1064))
+    for g in gallery_views(48):
+        if g.fractal == 0:
+            frames.append(("p_" + g.name, g.cx, g.cy, g.width, g.height, g.depth,
+                           parse_num(g.size), max(g.precision, 128)))
+    for name, scx, scy, W, H, depth, width, prec in frames:
+        cx = MpVal.from_fraction(parse_num(scx), prec).to_fraction()
+        cy = MpVal.from_fraction(parse_num(scy), prec).to_fraction()
+        width = MpVal.from_fraction(width, prec).to_fraction()
+        t0 = time.time()
+        cre, cim = [], []
+        for ln in range(H):
+            for ix in range(W):
+                x, y = perturb_c(cx, cy, width, W, H, ix, ln)
+                cre.append(hexfloat(x))
+                cim.append(hexfloat(y))
+        c1, m1 = O.points_mpfr(cre, cim, depth, prec, threads=THREADS)
+        c2, m2 = O.points_mpfr(cre, cim, depth, 2 * prec, threads=THREADS)
+        out[name] = c2.reshape(H, W).astype(np.int32)
+        out[name + "__p"] = c1.reshape(H, W).astype(np.int32)
+        out[name + "__mag"] = m2.reshape(H, W)
+        meta[name] = dict(cx=hexfloat(cx), cy=hexfloat(cy), width=hexfloat(width), W=W, H=H,
+                          depth=depth, prec=prec, oracle_prec=2 * prec)
+        print(f"{name}: {time.time() - t0:.1f}s confirmed {(c1 == c2).mean():.4f}")
+    # config 4: 4096 seeded sample pixels of the full frame, MPFR at 2176 bits
+    v = views["c4"]
+    cx, cy = parse_num(v["cx"]), parse_num(v["cy"])
+    width = parse_num(v["size"])
+    W, H, depth = v["width"], v["height"], v["depth"]
+    rng = np.random.Generator(np.random.PCG64(4004))
+    ix = rng.integers(0, W, 4096)
+    ln = rng.integers(0, H, 4096)
+    cre, cim = [], []
+    for a, b in zip(ix, ln):
+        x, y = perturb_c(cx, cy, width, W, H, int(a), int(b))
+        cre.append(hexfloat(x))
+        cim.append(hexfloat(y))
+    t0 = time.time()
+    counts, mag = O.points_mpfr(cre, cim, depth, 2176, threads=THREADS)
+    print(f"c4 samples at 2176 bits: {time.time() - t0:.1f}s")
+    out["c4_ix"], out["c4_line"] = ix.astype(np.int32), ln.astype(np.int32)
+    out["c4_counts"], out["c4_mag"] = counts.astype(np.int64), mag
+    meta["c4"] = dict(W=W, H=H, depth=depth, oracle_prec=2176, samples=4096, seed=4004)
+    np.savez_compressed(GOLD / "perturb.npz", **out)
+    (GOLD / "perturb_views.json").write_text(json.dumps(meta, indent=1))
+
+
+def parse_num(s):
+    from mdz_gb300.mpval import parse_number
+    return parse_number(s)
+
+
+def make_abi() -> None:
+    """abi_layout.json: offsets of image_info / rthdata from the reference
+    headers, as compiled by gcc here (LP64)."""
+    import tempfile
+    sys.path.insert(0, str(ROOT / "tests"))
+    import test_abi_cpu as T
+    with tempfile.TemporaryDirectory() as d:
+        offs = T.reference_layout(Path(d))
+    (GOLD / "abi_layout.json").write_text(json.dumps(
+        {"source": "gcc -std=gnu99 on src/image_info.h + src/render_threads.h (LP64)",
+         "offsets": offs}))
+
+
+def main(argv: list[str]) -> None:
+    from oracle import build as ob
+    ob.build()
+    what = argv[1:] or ["fp64"]
+    for w in what:
+        {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
+         "perturb": make_perturb}[w]()
+
+
+if __name__ == "__main__":
+    main(sys.argv)
