@@ -162,6 +162,7 @@ class DropIn:
         """render_to_file's loop: start, wait per line, process, until done."""
         lib, rth = self.lib, self.rth_ptr
         lib.rth_ui_start_render(rth)
+        lib.rth_ui_wait_until_started(rth)   # as gui_start_rendering does
         drawn_order = []
         t0 = time.time()
         y = 0

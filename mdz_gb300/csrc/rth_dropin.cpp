@@ -578,6 +578,17 @@ void rth_ui_start_render(mdz_rthdata* rth)
     mdz_rth_private* d = rth->data;
     memset(rth->lines_drawn, 0, (size_t)rth->img->user_height);
     rth->min_line_drawn = 0;
+    // Reset the progress of the previous frame here, not only when the new
+    // render thread starts: a caller that waits for lines straight after
+    // this call (render.c:49-51) must not see the last frame as finished.
+    pthread_mutex_lock(&d->lines_mutex);
+    memset(d->lines_rendered, 0, (size_t)rth->img->user_height);
+    d->total_lines_rendered = 0;
+    d->min_line_rendered = 0;
+    pthread_mutex_unlock(&d->lines_mutex);
+    pthread_mutex_lock(&d->started_mutex);
+    d->started = 0;
+    pthread_mutex_unlock(&d->started_mutex);
     pthread_mutex_lock(&d->start_mutex);
     d->start = 1;
     pthread_cond_signal(&d->start_cond);
