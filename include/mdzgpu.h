@@ -199,6 +199,15 @@ int mdzgpu_perturb_spacing(const mdzgpu_mpval* width, int32_t W,
 /* Orbit digits chosen for a precision (ceil(precision / 28) + 1, >= 5). */
 int32_t mdzgpu_perturb_limbs(int64_t precision);
 
+/* Pixel coordinate tables of the multi-limb path: xs[ix] (ix < W) and
+ * ys[r] for line row0 + r (r < nrows), each the value
+ * fractal_mpfr_calculate_line computes with `precision`-bit MPFR roundings
+ * (src/fractal.c:167-186), in the kernel's fixed point (`words` each). */
+int mdzgpu_mp_coordinates(const mdzgpu_mpval* xmin, const mdzgpu_mpval* ymax,
+                          const mdzgpu_mpval* width, int32_t W, int32_t row0,
+                          int32_t nrows, int64_t precision, int32_t words,
+                          uint32_t* xs, uint32_t* ys);
+
 /* Fixed-point helpers exposed for tests: convert an mpval to the kernel's
  * fixed-point words (out has `words` entries); 0 ok, MDZGPU_ERR_RANGE. */
 int mdzgpu_fx_from_mpval(const mdzgpu_mpval* v, int32_t words, uint32_t* out);

@@ -372,25 +372,12 @@ static int mp_tables(const uint32_t* xmin, const uint32_t* ymax, const uint32_t*
 
 namespace mdz {
 
-int mp_render_fixed(mdzgpu_ctx* ctx, const mdzgpu_frame* f, int words, const uint32_t* fxmin,
-                    const uint32_t* fymax, const uint32_t* fwidth, const uint32_t* fjre,
-                    const uint32_t* fjim, int32_t* d_out, int32_t* h_out, mdzgpu_stats* st,
-                    double t0)
+int mp_render_tables(mdzgpu_ctx* ctx, const mdzgpu_frame* f, int words,
+                     const std::vector<uint32_t>& tab, int32_t* d_out, int32_t* h_out,
+                     mdzgpu_stats* st, double t0)
 {
     int rc;
     const int W = f->width, H = f->height;
-    std::vector<uint32_t> tab;
-    if ((rc = mp_tables(fxmin, fymax, fwidth, W, H, words, tab))) {
-        set_error("multi-limb path: coordinates must satisfy |x|, |y| < 4");
-        return rc;
-    }
-    tab.resize(tab.size() + 2 * (size_t)words);
-    memcpy(&tab[(size_t)(W + H) * words], fjre, words * sizeof(uint32_t));
-    memcpy(&tab[(size_t)(W + H + 1) * words], fjim, words * sizeof(uint32_t));
-    if (f->family == MDZ_FAMILY_JULIA && (!fx_fits_coordinate(fjre, words) || !fx_fits_coordinate(fjim, words))) {
-        set_error("multi-limb path: julia constant must satisfy |c| < 4");
-        return MDZGPU_ERR_RANGE;
-    }
     const size_t n = (size_t)W * H;
     if (!d_out) {
         if ((rc = ctx->counts.ensure(n * sizeof(int32_t))))
@@ -460,15 +447,22 @@ static int mp_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval*
                   mdzgpu_mp_max_words());
         return MDZGPU_ERR_UNSUPPORTED;
     }
-    std::vector<uint32_t> a(w), b(w), c(w), jr(w), ji(w);
-    if (fx_from_mpval(xmin, w, a.data()) || fx_from_mpval(ymax, w, b.data())
-        || fx_from_mpval(width, w, c.data()) || fx_from_mpval(jre, w, jr.data())
-        || fx_from_mpval(jim, w, ji.data())) {
-        set_error("multi-limb path: value outside the fixed-point range");
+    // x[ix], y[line] and the julia constant exactly as MPFR computes them
+    // at `precision` bits (src/fractal.c:159-203)
+    const int W = f->width, H = f->height;
+    std::vector<uint32_t> tab((size_t)(W + H + 2) * w, 0);
+    int rc2 = mpfr_coordinate_tables(xmin, ymax, width, W, 0, H, (long)precision, w, tab.data(),
+                                     tab.data() + (size_t)W * w);
+    if (!rc2 && f->family == MDZ_FAMILY_JULIA)
+        rc2 = mpfr_round_to_fixed(jre, (long)precision, w, tab.data() + (size_t)(W + H) * w)
+              | mpfr_round_to_fixed(jim, (long)precision, w, tab.data() + (size_t)(W + H + 1) * w);
+    if (rc2 || (f->family == MDZ_FAMILY_JULIA
+                && (!fx_fits_coordinate(tab.data() + (size_t)(W + H) * w, w)
+                    || !fx_fits_coordinate(tab.data() + (size_t)(W + H + 1) * w, w)))) {
+        set_error("multi-limb path: coordinates must satisfy |x|, |y| < 4");
         return MDZGPU_ERR_RANGE;
     }
-    return mp_render_fixed(ctx, f, w, a.data(), b.data(), c.data(), jr.data(), ji.data(), d_out,
-                           h_out, st, t0);
+    return mp_render_tables(ctx, f, w, tab, d_out, h_out, st, t0);
 }
 
 int mdzgpu_render_mp(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* xmin,
@@ -496,6 +490,16 @@ int mdzgpu_render_mp_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu
     }
     return mp_common(ctx, f, xmin, ymax, width, julia_re, julia_im, precision, words, d_counts,
                      nullptr, st);
+}
+
+int mdzgpu_mp_coordinates(const mdzgpu_mpval* xmin, const mdzgpu_mpval* ymax,
+                          const mdzgpu_mpval* width, int32_t W, int32_t row0, int32_t nrows,
+                          int64_t precision, int32_t words, uint32_t* xs, uint32_t* ys)
+{
+    if (!xs || !ys || W <= 0 || nrows < 0 || words < 4)
+        return MDZGPU_ERR_ARG;
+    return mpfr_coordinate_tables(xmin, ymax, width, W, row0, nrows, (long)precision, words, xs,
+                                  ys);
 }
 
 int mdzgpu_fx_from_mpval(const mdzgpu_mpval* v, int32_t words, uint32_t* out)
@@ -560,13 +564,20 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         return rc;
     const size_t n = (size_t)f->width * f->height;
     const size_t entries = (size_t)f->depth + 2;
-    // orbit layout: zf[entries] float2 | zd[entries] double2 | ze[entries] int | len
-    const size_t off_zd = ((entries * sizeof(float2)) + 255) & ~(size_t)255;
-    const size_t off_ze = off_zd + (((entries * sizeof(double2)) + 255) & ~(size_t)255);
-    const size_t off_len = off_ze + (((entries * sizeof(int)) + 255) & ~(size_t)255);
+    // orbit layout (256-byte aligned pieces):
+    //   zf[entries] float2 | zd[entries] double2 | ze[entries] int |
+    //   dd[entries] double | de[entries] int | len | centre digits | rebases |
+    //   digits[entries][2][L] int (raw orbit, scratch)
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t off_zd = al(entries * sizeof(float2));
+    const size_t off_ze = off_zd + al(entries * sizeof(double2));
+    const size_t off_dd = off_ze + al(entries * sizeof(int));
+    const size_t off_de = off_dd + al(entries * sizeof(double));
+    const size_t off_len = off_de + al(entries * sizeof(int));
     const size_t off_dig = off_len + 256;
-    const size_t off_reb = off_dig + ((2 * L * sizeof(int) + 255) & ~(size_t)255);
-    const size_t orbit_bytes = off_reb + 256;
+    const size_t off_reb = off_dig + al(2 * L * sizeof(int));
+    const size_t off_raw = off_reb + 256;
+    const size_t orbit_bytes = off_raw + al(entries * 2 * (size_t)L * sizeof(int));
     if ((rc = ctx->orbit.ensure(orbit_bytes)) || (rc = ctx->sync.ensure(sizeof(FrameSync))))
         return rc;
     if (!d_out) {
@@ -593,6 +604,9 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.zf = (float2*)ob;
     o.zd = (double2*)(ob + off_zd);
     o.ze = (int*)(ob + off_ze);
+    o.dd = (double*)(ob + off_dd);
+    o.de = (int*)(ob + off_de);
+    o.digits = (int*)(ob + off_raw);
     o.max_k = (int)f->depth + 1;
     o.out_len = (int*)(ob + off_len);
     cudaEvent_t evo;
@@ -614,6 +628,8 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.zf = o.zf;
     p.zd = o.zd;
     p.ze = o.ze;
+    p.dd = o.dd;
+    p.de = o.de;
     p.orbit_len = o.out_len;
     p.out = d_out;
     p.mag = d_mag;
@@ -638,7 +654,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     int olen = 0;
     MDZ_CUDA_TRY(cudaMemcpyAsync(&reb, p.rebases, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(&olen, o.out_len, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    rc = finish_stats(ctx, st, t0, 2, (int64_t)dig.size() * 4, d2h + 12);
+    rc = finish_stats(ctx, st, t0, 3, (int64_t)dig.size() * 4, d2h + 12);
     if (!rc && st) {
         float oms = 0.f;
         cudaEventElapsedTime(&oms, ctx->ev0, evo);

@@ -109,9 +109,12 @@ struct OrbitLaunch {
     int limbs;              // L radix-2^28 signed digits, F = 28 (L - 1)
     const int* c_re;        // [L] centre, balanced signed digits
     const int* c_im;
+    int* digits;            // [max_k + 1][2][L] raw digits of every Z_k
     float2* zf;             // [max_k + 1] Z_k in FP32
     double2* zd;            // [max_k + 1] Z_k mantissas in FP64 ...
     int* ze;                // ... times 2^ze[k]
+    double* dd;             // [max_k + 1] D_k = |Z_k|^2 - 4 = dd * 2^de
+    int* de;
     int max_k;              // last index computed (depth + 1)
     int* out_len;           // number of valid entries (device)
 };
@@ -126,6 +129,8 @@ struct PerturbLaunch {
     const float2* zf;
     const double2* zd;
     const int* ze;
+    const double* dd;
+    const int* de;
     const int* orbit_len;   // device: valid orbit entries
     int32_t* out;
     float* mag;             // |z|^2 at escape (may be null)
@@ -152,10 +157,14 @@ int digits28_from_mpval(const mdzgpu_mpval* v, int L, int* out);
 // Half pixel spacing width / (2 W) rounded to 40 significant bits.
 int half_spacing(const mdzgpu_mpval* width, int W, double* hs_m, int* hs_e);
 int mp_words_for_precision(long precision);
-// Multi-limb render from fixed-point inputs (used by the drop-in layer).
-int mp_render_fixed(mdzgpu_ctx* ctx, const mdzgpu_frame* f, int words, const uint32_t* fxmin,
-                    const uint32_t* fymax, const uint32_t* fwidth, const uint32_t* fjre,
-                    const uint32_t* fjim, int32_t* d_out, int32_t* h_out, mdzgpu_stats* st,
-                    double t0);
+// Pixel coordinate tables of the MPFR path at precision p: x[ix] for
+// ix < W and y[row0 + r] for r < nrows, each the p-bit value
+// fractal_mpfr_calculate_line computes, converted to fixed point.
+int mpfr_coordinate_tables(const mdzgpu_mpval* xmin, const mdzgpu_mpval* ymax,
+                           const mdzgpu_mpval* width, int W, int row0, int nrows, long p,
+                           int words, uint32_t* xs, uint32_t* ys);
+// A value rounded to p bits (mpfr_set into a p-bit variable), as fixed point.
+int mpfr_round_to_fixed(const mdzgpu_mpval* v, long p, int words, uint32_t* out);
+
 
 }  // namespace mdz

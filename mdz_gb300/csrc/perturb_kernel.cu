@@ -49,11 +49,12 @@ __device__ __forceinline__ void digit_split(long long v, long long& digit, long 
     carry = (v - digit) >> 28;
 }
 
-// value of 4 digits starting at `top` (inclusive, downwards) as a double
-// mantissa m and exponent x: value ~ m * 2^x, |m| in [0.5, 1) unless zero.
-__device__ void limbs_to_double(const int* d, int L, double& m, int& x)
+// value of the 4 digits below the top nonzero one as a double mantissa m and
+// exponent x: value ~ m * 2^x, |m| in [0.5, 1) unless zero.  `scale` is the
+// binary weight of digit 0.
+__device__ void digits_to_double(const int* d, int n, int scale, double& m, int& x)
 {
-    int top = L - 1;
+    int top = n - 1;
     while (top > 0 && d[top] == 0)
         --top;
     double v = (double)d[top];
@@ -63,16 +64,20 @@ __device__ void limbs_to_double(const int* d, int L, double& m, int& x)
         v += ldexp((double)d[top - 2], -56);
     if (top >= 3)
         v += ldexp((double)d[top - 3], -84);
-    // v * 2^(28 top - F)
     int ex = 0;
     m = frexp(v, &ex);
-    x = ex + 28 * top - 28 * (L - 1);
+    x = ex + 28 * top + scale;
     if (v == 0.0) {
         m = 0.0;
         x = 0;
     }
 }
 
+// The serial part: one warp iterates Z_{k+1} = Z_k^2 + C and stores the raw
+// digits of every Z_k (re then im, L each) to HBM.  Everything else about
+// each Z_k (FP64 / FP32 roundings, |Z_k|^2 - 4) is done afterwards by
+// orbit_finish_kernel, in parallel over k, so this loop carries only the
+// multi-limb arithmetic.
 __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
 {
     __shared__ int zr[kMaxOrbitLimbs], zi[kMaxOrbitLimbs], cr[kMaxOrbitLimbs], ci[kMaxOrbitLimbs];
@@ -83,51 +88,27 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
         ci[j] = p.c_im[j];
         zr[j] = p.c_re[j];
         zi[j] = p.c_im[j];
+        p.digits[j] = 0;                    // Z_0 = 0
+        p.digits[L + j] = 0;
+        p.digits[2 * L + j] = p.c_re[j];    // Z_1 = C
+        p.digits[3 * L + j] = p.c_im[j];
     }
     __syncwarp();
-    // Z_0 = 0, Z_1 = C
-    if (lane == 0) {
-        p.zf[0] = make_float2(0.f, 0.f);
-        p.zd[0] = make_double2(0.0, 0.0);
-        p.ze[0] = 0;
-    }
     const int cbase = L - 4;       // lowest column computed (3 guard columns)
     const int ctop = 2 * L - 2;    // highest column
     int k = 1;
-    int escaped = 0;
     for (;; ++k) {
-        // ---- store Z_k ----
-        double mr = 0.0, mi = 0.0;
-        int xr = 0, xi = 0;
-        if (lane == 0)
-            limbs_to_double(zr, L, mr, xr);
-        if (lane == 1)
-            limbs_to_double(zi, L, mi, xi);
-        mi = __shfl_sync(0xffffffffu, mi, 1);
-        xi = __shfl_sync(0xffffffffu, xi, 1);
+        // escape test on the two top digits (FP32 is enough to stop the
+        // orbit: stopping a step early or late only moves a rebase)
+        int escaped = 0;
         if (lane == 0) {
-            // common exponent for the pair
-            const int xe = (mr == 0.0) ? xi : (mi == 0.0 ? xr : max(xr, xi));
-            const double dr = ldexp(mr, xr - xe);
-            const double di = ldexp(mi, xi - xe);
-            // store with exponent 0 whenever the plain double is normal
-            int store_e = 0;
-            double sr = ldexp(dr, xe), si = ldexp(di, xe);
-            if (xe < -960) {
-                store_e = xe;
-                sr = dr;
-                si = di;
-            }
-            p.zd[k] = make_double2(sr, si);
-            p.ze[k] = store_e;
-            p.zf[k] = make_float2((float)ldexp(dr, xe), (float)ldexp(di, xe));
-            const double vr = ldexp(dr, xe), vi = ldexp(di, xe);
-            escaped = (vr * vr + vi * vi > 4.0) ? 1 : 0;
+            const float a = (float)zr[L - 1] + (float)zr[L - 2] * 3.7252903e-9f;
+            const float b = (float)zi[L - 1] + (float)zi[L - 2] * 3.7252903e-9f;
+            escaped = a * a + b * b > 4.0f;
         }
         escaped = __shfl_sync(0xffffffffu, escaped, 0);
         if (escaped || k >= p.max_k)
             break;
-        // ---- Z_{k+1} = Z_k^2 + C ----
         long long vr[3], vi[3];
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
@@ -148,11 +129,9 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
             long long dr = 0, di = 0;
             if (!(c & 1)) {
                 const int h = c >> 1;
-                if (h <= L - 1) {
-                    const long long a = zr[h], b = zi[h];
-                    dr = a * a - b * b;
-                    di = a * b;
-                }
+                const long long a = zr[h], b = zi[h];
+                dr = a * a - b * b;
+                di = a * b;
             }
             vr[s] = 2 * pr + dr;
             vi[s] = 2 * (pi + di);
@@ -161,8 +140,8 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
                 vi[s] += ci[c - (L - 1)];
             }
         }
-        // ---- carry propagation: three passes, column c+1 is lane+1 (slot
-        // s) or lane 0 of slot s+1 ----
+        // carry propagation: three passes; column c+1 is lane+1 (slot s) or
+        // lane 0 of slot s+1
 #pragma unroll
         for (int pass = 0; pass < 3; ++pass) {
             long long dgr[3], dgi[3], cyr[3], cyi[3];
@@ -186,18 +165,90 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
             }
         }
         __syncwarp();
+        int* out = p.digits + (size_t)(k + 1) * 2 * L;
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
             const int c = cbase + lane + 32 * s;
             if (c <= ctop && c >= L - 1) {
                 zr[c - (L - 1)] = (int)vr[s];
                 zi[c - (L - 1)] = (int)vi[s];
+                out[c - (L - 1)] = (int)vr[s];
+                out[L + c - (L - 1)] = (int)vi[s];
             }
         }
         __syncwarp();
     }
     if (lane == 0)
         *p.out_len = k + 1;  // entries 0..k are valid
+}
+
+// Per entry k (one thread each): the FP64 pair with its exponent, the FP32
+// pair, and D_k = |Z_k|^2 - 4 -- from FP64 when that is far from 0,
+// otherwise exactly from the digits (the full 2L-column sum of squares),
+// because the escape test of a pixel with a tiny dz needs the sign of
+// D_k + 2 Re(conj(Z_k) dz) + |dz|^2 and FP32 / FP64 roundings of Z_k can
+// not give it when |Z_k| is within 2^-20 of 2.
+__global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int len = *p.out_len;
+    if (k >= len)
+        return;
+    const int L = p.limbs;
+    const int* dr = p.digits + (size_t)k * 2 * L;
+    const int* di = dr + L;
+    const int F = 28 * (L - 1);
+    double mr, mi;
+    int xr, xi;
+    digits_to_double(dr, L, -F, mr, xr);
+    digits_to_double(di, L, -F, mi, xi);
+    const int xe = (mr == 0.0) ? xi : (mi == 0.0 ? xr : max(xr, xi));
+    const double nr = ldexp(mr, xr - xe), ni = ldexp(mi, xi - xe);
+    const double vr = ldexp(nr, xe), vi = ldexp(ni, xe);
+    if (xe < -960) {
+        p.zd[k] = make_double2(nr, ni);
+        p.ze[k] = xe;
+    } else {
+        p.zd[k] = make_double2(vr, vi);
+        p.ze[k] = 0;
+    }
+    p.zf[k] = make_float2((float)vr, (float)vi);
+    const double d_approx = vr * vr + vi * vi - 4.0;
+    if (fabs(d_approx) > 9.5367431640625e-7 /* 2^-20 */) {
+        p.dd[k] = d_approx;
+        p.de[k] = 0;
+        return;
+    }
+    // exact: columns of Zr^2 + Zi^2 (weight of column c: 2^(28 c - 2F)),
+    // minus 4 in the top column, carries resolved serially
+    long long col[2 * kMaxOrbitLimbs];
+    int dig[2 * kMaxOrbitLimbs];
+    const int ncol = 2 * L - 1;
+    for (int c = 0; c < ncol; ++c) {
+        long long acc = 0;
+        const int ilo = c - (L - 1) > 0 ? c - (L - 1) : 0;
+        const int ihi = c < L - 1 ? c : L - 1;
+        for (int i = ilo; i <= ihi; ++i)
+            acc += (long long)dr[i] * dr[c - i] + (long long)di[i] * di[c - i];
+        col[c] = acc;
+    }
+    col[ncol - 1] -= 4;
+    long long carry = 0;
+    for (int c = 0; c < ncol; ++c) {
+        long long v = col[c] + carry, d, cy;
+        digit_split(v, d, cy);
+        dig[c] = (int)d;
+        carry = cy;
+    }
+    // anything left in `carry` is a multiple of 2^(28 ncol - 2F) = 2^28
+    // above the top column: fold it back in (|D| < 1 here, so it is 0 or a
+    // single unit that cancels the top digit)
+    dig[ncol - 1] += (int)(carry << 28);
+    double m;
+    int x;
+    digits_to_double(dig, ncol, -2 * F, m, x);
+    p.dd[k] = m;
+    p.de[k] = x;
 }
 
 // --------------------------------------------------------------------------
@@ -305,7 +356,23 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
         const float zr = fmaf(st.s, st.tr, Z.x);
         const float zi = fmaf(st.s, st.ti, Z.y);
         mag = fmaf(zr, zr, zi * zi);
-        if (mag > 4.0f) {
+        bool esc = mag > 4.0f;
+        if (fabsf(mag - 4.0f) < 6.1035156e-5f /* 2^-14 */) {
+            // |z|^2 - 4 = D_m + 2 Re(conj(Z_m) dz) + |dz|^2, in FP64 with
+            // explicit exponents (D_m exact from the orbit digits)
+            const double2 zd = p.zd[m];
+            const int ze = p.ze[m];
+            const double dd = p.dd[m];
+            const int de = p.de[m];
+            const double t2 = 2.0 * (zd.x * (double)st.tr + zd.y * (double)st.ti);
+            const int e2 = ze + st.e;
+            const double t3 = (double)st.tr * st.tr + (double)st.ti * st.ti;
+            const int e3 = 2 * st.e;
+            const int E = max(max(dexp_of(dd) + de, dexp_of(t2) + e2), dexp_of(t3) + e3);
+            const double v = ldexp(dd, de - E) + ldexp(t2, e2 - E) + ldexp(t3, e3 - E);
+            esc = v > 0.0;
+        }
+        if (esc) {
             mag_out = mag;
             return wz;
         }
@@ -403,6 +470,8 @@ int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
         return MDZGPU_ERR_UNSUPPORTED;
     }
     orbit_kernel<<<1, 32, 0, s>>>(p);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    orbit_finish_kernel<<<(p.max_k + 1 + 127) / 128, 128, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
     return MDZGPU_OK;
 }

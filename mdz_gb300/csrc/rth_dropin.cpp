@@ -118,8 +118,70 @@ int device_index()
     return s ? atoi(s) : 0;
 }
 
-// Builds the launch for the whole frame; returns the method's fixed-point
-// tables in `tab` (MP methods).
+mdzgpu_mpval as_mpval(const mdz_mpfr* v)
+{
+    mdzgpu_mpval m;
+    m.sign = v->sign < 0 ? -1 : 1;
+    m.exp = v->exp;
+    m.nlimbs = v->exp == MDZ_MPFR_EXP_ZERO ? 0 : (int32_t)((v->prec + 63) / 64);
+    m.d = m.nlimbs ? v->d : nullptr;
+    return m;
+}
+
+// Fixed-point tables for rows [row0, row0 + nrows): x[W] | y[nrows] |
+// julia c_re | c_im.  MPFR callback: MPFR's own p-bit coordinate roundings
+// (src/fractal.c:159-203).  GMP callback: exact values from gxmin / gymax /
+// gwidth (src/fractal.c:299-332 reads those).
+bool frame_tables(const mdz_image_info* img, Method method, int words, int row0, int nrows,
+                  std::vector<uint32_t>& tab)
+{
+    const int W = img->real_width;
+    uint32_t* xs = tab.data();
+    uint32_t* ys = xs + (size_t)W * words;
+    uint32_t* jc = ys + (size_t)nrows * words;
+    int rc = 0;
+    if (method == M_MPFR) {
+        if (img->xmin->exp == MDZ_MPFR_EXP_NAN || img->ymax->exp == MDZ_MPFR_EXP_NAN
+            || img->width->exp == MDZ_MPFR_EXP_NAN) {
+            set_error("view coordinates are NaN");
+            return false;
+        }
+        const mdzgpu_mpval a = as_mpval(img->xmin), b = as_mpval(img->ymax),
+                           c = as_mpval(img->width);
+        rc = mpfr_coordinate_tables(&a, &b, &c, W, row0, nrows, img->precision, words, xs, ys);
+        if (!rc && img->family == MDZ_FAMILY_JULIA) {
+            const mdzgpu_mpval jr = as_mpval(img->u.julia.c_re), ji = as_mpval(img->u.julia.c_im);
+            rc = mpfr_round_to_fixed(&jr, img->precision, words, jc)
+                 | mpfr_round_to_fixed(&ji, img->precision, words, jc + words);
+        }
+    } else {
+        std::vector<uint32_t> a(words), b(words), c(words);
+        rc = fx_from_mpf(img->gxmin, words, a.data()) | fx_from_mpf(img->gymax, words, b.data())
+             | fx_from_mpf(img->gwidth, words, c.data());
+        if (!rc) {
+            for (int ix = 0; ix < W; ++ix)
+                fx_affine(a.data(), c.data(), ix, W, +1, words, xs + (size_t)ix * words);
+            for (int r = 0; r < nrows; ++r)
+                fx_affine(b.data(), c.data(), row0 + r, W, -1, words, ys + (size_t)r * words);
+            if (img->family == MDZ_FAMILY_JULIA)
+                rc = fx_from_mpfr(img->u.julia.c_re, words, jc)
+                     | fx_from_mpfr(img->u.julia.c_im, words, jc + words);
+        }
+    }
+    if (rc) {
+        set_error("multi-limb path: view outside the fixed-point range (|x|, |y| < 4)");
+        return false;
+    }
+    for (size_t k = 0; k < (size_t)(W + nrows + 2); ++k)
+        if (!fx_fits_coordinate(&tab[k * words], words)) {
+            set_error("multi-limb path: coordinates must satisfy |x|, |y| < 4");
+            return false;
+        }
+    return true;
+}
+
+// Renders the whole frame with one kernel launch, publishing rows as their
+// 4-row bands complete.
 int gpu_frame(mdz_rthdata* rth, Method method)
 {
     mdz_rth_private* d = rth->data;
@@ -200,34 +262,11 @@ int gpu_frame(mdz_rthdata* rth, Method method)
             fail_remaining(rth, row_done);
             return 0;
         }
-        std::vector<uint32_t> a(words), b(words), c(words), jr(words, 0), ji(words, 0);
-        if (method == M_MPFR)
-            rc = fx_from_mpfr(img->xmin, words, a.data()) | fx_from_mpfr(img->ymax, words, b.data())
-                 | fx_from_mpfr(img->width, words, c.data());
-        else
-            rc = fx_from_mpf(img->gxmin, words, a.data()) | fx_from_mpf(img->gymax, words, b.data())
-                 | fx_from_mpf(img->gwidth, words, c.data());
-        if (img->family == MDZ_FAMILY_JULIA)
-            rc |= fx_from_mpfr(img->u.julia.c_re, words, jr.data())
-                  | fx_from_mpfr(img->u.julia.c_im, words, ji.data());
-        if (rc) {
-            set_error("view outside the fixed-point range");
+        std::vector<uint32_t> tab((size_t)(W + H + 2) * words, 0);
+        if (!frame_tables(img, method, words, 0, H, tab)) {
             fail_remaining(rth, row_done);
             return 0;
         }
-        std::vector<uint32_t> tab((size_t)(W + H + 2) * words);
-        for (int ix = 0; ix < W; ++ix)
-            fx_affine(a.data(), c.data(), ix, W, +1, words, &tab[(size_t)ix * words]);
-        for (int y = 0; y < H; ++y)
-            fx_affine(b.data(), c.data(), y, W, -1, words, &tab[(size_t)(W + y) * words]);
-        memcpy(&tab[(size_t)(W + H) * words], jr.data(), words * 4);
-        memcpy(&tab[(size_t)(W + H + 1) * words], ji.data(), words * 4);
-        for (size_t k = 0; k < (size_t)(W + H + 2); ++k)
-            if (!fx_fits_coordinate(&tab[k * words], words)) {
-                set_error("multi-limb path: coordinates must satisfy |x|, |y| < 4");
-                fail_remaining(rth, row_done);
-                return 0;
-            }
         if ((rc = ctx->coords.ensure(tab.size() * 4))
             || cudaMemcpyAsync(ctx->coords.ptr, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, s)
                    != cudaSuccess
@@ -459,26 +498,9 @@ int line_render(mdz_image_info* img, int line, Method method)
             }
         if (words < 0)
             return 0;
-        std::vector<uint32_t> a(words), b(words), c(words), tab((size_t)(W + 3) * words, 0);
-        if (method == M_MPFR)
-            rc = fx_from_mpfr(img->xmin, words, a.data()) | fx_from_mpfr(img->ymax, words, b.data())
-                 | fx_from_mpfr(img->width, words, c.data());
-        else
-            rc = fx_from_mpf(img->gxmin, words, a.data()) | fx_from_mpf(img->gymax, words, b.data())
-                 | fx_from_mpf(img->gwidth, words, c.data());
-        if (img->family == MDZ_FAMILY_JULIA)
-            rc |= fx_from_mpfr(img->u.julia.c_re, words, &tab[(size_t)(W + 1) * words])
-                  | fx_from_mpfr(img->u.julia.c_im, words, &tab[(size_t)(W + 2) * words]);
-        if (rc)
+        std::vector<uint32_t> tab((size_t)(W + 3) * words, 0);
+        if (!frame_tables(img, method, words, line, 1, tab))
             return 0;
-        for (int ix = 0; ix < W; ++ix)
-            fx_affine(a.data(), c.data(), ix, W, +1, words, &tab[(size_t)ix * words]);
-        fx_affine(b.data(), c.data(), line, W, -1, words, &tab[(size_t)W * words]);
-        for (int k = 0; k < W + 3; ++k)
-            if (!fx_fits_coordinate(&tab[(size_t)k * words], words)) {
-                set_error("multi-limb path: coordinates must satisfy |x|, |y| < 4");
-                return 0;
-            }
         if (ctx->coords.ensure(tab.size() * 4)
             || cudaMemcpyAsync(ctx->coords.ptr, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice,
                                ctx->stream) != cudaSuccess)

@@ -63,6 +63,8 @@ _SIGS = {
     "mdzgpu_perturb_limbs": (C.c_int32, [C.c_int64]),
     "mdzgpu_mp_max_words": (C.c_int32, []),
     "mdzgpu_fx_from_mpval": (C.c_int, [C.POINTER(MpValStruct), C.c_int32, P]),
+    "mdzgpu_mp_coordinates": (C.c_int, [C.POINTER(MpValStruct)] * 3
+                              + [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int32, P, P]),
     "mdzgpu_abi_layout": (C.c_int, [P, C.c_int]),
     "mdzgpu_measure_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     # drop-in layer

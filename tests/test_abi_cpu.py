@@ -138,3 +138,46 @@ def test_perturb_spacing_is_40_bits():
     hs = Fraction(m) * Fraction(2) ** e
     exact = Fraction(1, 2 ** 1000) / 3840
     assert abs(hs - exact) / exact < Fraction(1, 2 ** 39)
+
+
+def mpfr_pixel_c(rect, W, prec, ix, line):
+    """fractal_mpfr_calculate_line's c (src/fractal.c:167-186), each MPFR
+    call an exact operation rounded to nearest at `prec` bits."""
+    def rn(x):
+        return MpVal.from_fraction(x, prec).to_fraction()
+    width, xmin, ymax = (rn(v.to_fraction()) for v in (rect.width, rect.xmin, rect.ymax))
+    y = rn(ymax - rn(rn(width / W) * line))
+    x = rn(rn(rn(Fraction(ix, W)) * width) + xmin)
+    return x, y
+
+
+@pytest.mark.parametrize("prec,cx,cy,size,W,H", [
+    (80, "-1.7495931476527795538", "5.79e-8", "2.3e-17", 40, 30),
+    (128, "-0.7436447860", "0.1318252536", "1e-30", 33, 17),
+    (256, "0.3750001", "-0.44", "0x1p-200", 64, 48),
+    (1088, "-0.1592", "1.0317", "0x1p-1000", 24, 12),
+])
+def test_mp_coordinates_equal_mpfr_roundings(prec, cx, cy, size, W, H):
+    from mdz_gb300.views import mdz_rect
+    lib = native.load()
+    words = max(4, -(-(prec + 40) // 32))
+    words += words & 1
+    r = mdz_rect(W, H, prec, cx, cy, size)
+    xs = (C.c_uint32 * (W * words))()
+    ys = (C.c_uint32 * (H * words))()
+    args = [v.struct() for v in (r.xmin, r.ymax, r.width)]
+    assert lib.mdzgpu_mp_coordinates(*[C.byref(a) for a, _ in args], W, 0, H, prec, words,
+                                      xs, ys) == 0
+    F = 32 * words - 8
+
+    def fixed(arr, k):
+        v = sum(int(arr[k * words + i]) << (32 * i) for i in range(words))
+        if v >> (32 * words - 1):
+            v -= 1 << (32 * words)
+        return Fraction(v, 1 << F)
+    for ix in range(W):
+        x, _ = mpfr_pixel_c(r, W, prec, ix, 0)
+        assert fixed(xs, ix) == x
+    for ln in range(H):
+        _, y = mpfr_pixel_c(r, W, prec, 0, ln)
+        assert fixed(ys, ln) == y
