@@ -123,6 +123,8 @@ typedef struct mdzgpu_stats {
     double orbit_ms;        /* reference-orbit kernel time (perturbation) */
     int64_t rebases;        /* rebases taken (perturbation) */
     int64_t orbit_len;      /* reference orbit length (perturbation) */
+    int64_t escalated_fp64; /* pixels re-run with FP64 deltas (perturbation) */
+    int64_t escalated_mp;   /* pixels re-run on the multi-limb kernel */
 } mdzgpu_stats;
 
 /* An arbitrary-precision binary value with MPFR's meaning:

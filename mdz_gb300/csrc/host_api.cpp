@@ -227,6 +227,7 @@ void mdzgpu_destroy(mdzgpu_ctx* ctx)
     ctx->orbit.release();
     ctx->orbit_fx.release();
     ctx->aux.release();
+    ctx->lists.release();
     ctx->pinned.release();
     ctx->staging.release();
     cudaEventDestroy(ctx->ev0);
@@ -526,6 +527,46 @@ int32_t mdzgpu_perturb_limbs(int64_t precision)
     return (int32_t)L;
 }
 
+// Bits a pass may lose to rebase cancellation before its pixel is re-run by
+// the next, more precise pass (FP32 -> FP64 -> multi-limb).
+constexpr float kLostLimitFp32 = 4.0f;
+constexpr float kLostLimitFp64 = 20.0f;
+
+// Fixed-point pixel coordinates of the perturbation geometry for the
+// multi-limb pass: x[ix] = cx + (2 ix - W) hs, y[line] = cy + (H - 2 line) hs.
+static int perturb_tables(const mdzgpu_mpval* cx, const mdzgpu_mpval* cy, double hs_m, int hs_e,
+                          int W, int H, int words, std::vector<uint32_t>& tab)
+{
+    std::vector<uint32_t> fcx(words), fcy(words), fhs(words);
+    if (fx_from_mpval(cx, words, fcx.data()) || fx_from_mpval(cy, words, fcy.data()))
+        return MDZGPU_ERR_RANGE;
+    // hs = (hs_m 2^39) 2^(hs_e - 39), hs_m 2^39 an integer below 2^40
+    const uint64_t hint = (uint64_t)ldexp(hs_m, 39);
+    uint64_t limb[1] = {hint << 24};
+    mdzgpu_mpval hv;
+    hv.sign = 1;
+    hv.nlimbs = 1;
+    hv.exp = (int64_t)hs_e + 1;   // hint << 24 is normalised: 0.(hint<<24) 2^exp
+    hv.d = limb;
+    if (fx_from_mpval(&hv, words, fhs.data()))
+        return MDZGPU_ERR_RANGE;
+    for (int ix = 0; ix < W; ++ix) {
+        const long k = 2L * ix - W;
+        fx_affine(fcx.data(), fhs.data(), k < 0 ? -k : k, 1, k < 0 ? -1 : +1, words,
+                  tab.data() + (size_t)ix * words);
+        if (!fx_fits_coordinate(tab.data() + (size_t)ix * words, words))
+            return MDZGPU_ERR_RANGE;
+    }
+    for (int y = 0; y < H; ++y) {
+        const long k = (long)H - 2L * y;
+        fx_affine(fcy.data(), fhs.data(), k < 0 ? -k : k, 1, k < 0 ? -1 : +1, words,
+                  tab.data() + (size_t)(W + y) * words);
+        if (!fx_fits_coordinate(tab.data() + (size_t)(W + y) * words, words))
+            return MDZGPU_ERR_RANGE;
+    }
+    return MDZGPU_OK;
+}
+
 static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,
                           const mdzgpu_mpval* cy, const mdzgpu_mpval* width, int64_t precision,
                           int32_t limbs, int32_t* d_out, float* d_mag, int32_t* h_out,
@@ -609,6 +650,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.digits = (int*)(ob + off_raw);
     o.max_k = (int)f->depth + 1;
     o.out_len = (int*)(ob + off_len);
+    int64_t h2d_extra = 0;
     cudaEvent_t evo;
     MDZ_CUDA_TRY(cudaEventCreate(&evo));
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -636,9 +678,83 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.sync = (FrameSync*)ctx->sync.ptr;
     p.rebases = (unsigned long long*)(ob + off_reb);
     p.stop = nullptr;
-    if ((rc = launch_perturb(ctx, p, ctx->stream))) {
+    // escalation lists: [count1 | count2 | pad] list1[n] list2[n]
+    if ((rc = ctx->lists.ensure(256 + 2 * n * sizeof(unsigned)))) {
         cudaEventDestroy(evo);
         return rc;
+    }
+    unsigned* counts_dev = (unsigned*)ctx->lists.ptr;
+    unsigned* list1 = (unsigned*)((char*)ctx->lists.ptr + 256);
+    unsigned* list2 = list1 + n;
+    MDZ_CUDA_TRY(cudaMemsetAsync(ctx->lists.ptr, 0, 256, ctx->stream));
+    // pass 0: FP32 mantissas over the frame
+    p.lost_limit = kLostLimitFp32;
+    p.flag_out = list1;
+    p.flag_out_count = counts_dev;
+    if ((rc = launch_perturb(ctx, p, ctx->stream, 0))) {
+        cudaEventDestroy(evo);
+        return rc;
+    }
+    // pass 1: FP64 mantissas over the pixels pass 0 flagged
+    MDZ_CUDA_TRY(cudaMemsetAsync(&((FrameSync*)ctx->sync.ptr)->tile_counter, 0, sizeof(unsigned),
+                                 ctx->stream));
+    p.list_in = list1;
+    p.list_in_count = counts_dev;
+    p.lost_limit = kLostLimitFp64;
+    p.flag_out = list2;
+    p.flag_out_count = counts_dev + 1;
+    if ((rc = launch_perturb(ctx, p, ctx->stream, 1))) {
+        cudaEventDestroy(evo);
+        return rc;
+    }
+    // pass 2: the exact multi-limb kernel for what FP64 could not settle
+    {
+        const int words = mp_words_for_precision((long)precision);
+        int w = -1;
+        for (int k = words; k <= mdzgpu_mp_max_words(); ++k)
+            if (mp_words_supported(k)) {
+                w = k;
+                break;
+            }
+        if (w < 0)
+            w = mdzgpu_mp_max_words();
+        std::vector<uint32_t> tab((size_t)(f->width + f->height + 2) * w, 0);
+        if ((rc = perturb_tables(cx, cy, hs_m, hs_e, f->width, f->height, w, tab))) {
+            cudaEventDestroy(evo);
+            return rc;
+        }
+        if ((rc = ctx->coords.ensure(tab.size() * 4))) {
+            cudaEventDestroy(evo);
+            return rc;
+        }
+        MDZ_CUDA_TRY(cudaMemcpyAsync(ctx->coords.ptr, tab.data(), tab.size() * 4,
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        MDZ_CUDA_TRY(cudaMemsetAsync(&((FrameSync*)ctx->sync.ptr)->tile_counter, 0,
+                                     sizeof(unsigned), ctx->stream));
+        MpLaunch q;
+        q.W = f->width;
+        q.H = f->height;
+        q.row0 = 0;
+        q.nrows = f->height;
+        q.family = MDZ_FAMILY_MANDEL;
+        q.fractal = MDZ_MANDELBROT;
+        q.depth = (uint32_t)f->depth;
+        q.words = w;
+        q.xs = (const uint32_t*)ctx->coords.ptr;
+        q.ys = q.xs + (size_t)f->width * w;
+        q.julia = q.xs + (size_t)(f->width + f->height) * w;
+        q.out = d_out;
+        q.sync = (FrameSync*)ctx->sync.ptr;
+        q.tile_rows_done = nullptr;
+        q.band_flags = nullptr;
+        q.stop = nullptr;
+        q.list = list2;
+        q.list_count = counts_dev + 1;
+        if ((rc = launch_mp(ctx, q, ctx->stream))) {
+            cudaEventDestroy(evo);
+            return rc;
+        }
+        h2d_extra = (int64_t)tab.size() * 4;
     }
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
     int64_t d2h = 0;
@@ -652,10 +768,14 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     }
     unsigned long long reb = 0;
     int olen = 0;
+    unsigned esc[2] = {0, 0};
+    MDZ_CUDA_TRY(cudaMemcpyAsync(esc, counts_dev, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(&reb, p.rebases, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(&olen, o.out_len, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    rc = finish_stats(ctx, st, t0, 3, (int64_t)dig.size() * 4, d2h + 12);
+    rc = finish_stats(ctx, st, t0, 5, (int64_t)dig.size() * 4 + h2d_extra, d2h + 20);
     if (!rc && st) {
+        st->escalated_fp64 = esc[0];
+        st->escalated_mp = esc[1];
         float oms = 0.f;
         cudaEventElapsedTime(&oms, ctx->ev0, evo);
         st->orbit_ms = oms;

@@ -63,6 +63,7 @@ struct mdzgpu_ctx {
     mdz::DevBuf orbit;      // reference orbit (perturbation)
     mdz::DevBuf orbit_fx;   // fixed-point reference state
     mdz::DevBuf aux;        // per-pixel float output (perturbation)
+    mdz::DevBuf lists;      // escalation pixel lists (perturbation)
     mdz::PinnedBuf pinned;  // small host-mapped status words
     mdz::PinnedBuf staging; // pinned host copy of counts
 };
@@ -96,6 +97,10 @@ struct MpLaunch {
     unsigned int* tile_rows_done;
     volatile int* band_flags;
     volatile int* stop;
+    // list mode (perturbation escalation): render only the pixels listed,
+    // out[list[i]] with x = xs[list[i] % W], y = ys[list[i] / W]
+    const unsigned* list = nullptr;
+    const unsigned* list_count = nullptr;
 };
 int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
 bool mp_words_supported(int words);
@@ -137,8 +142,16 @@ struct PerturbLaunch {
     FrameSync* sync;
     unsigned long long* rebases;
     volatile int* stop;
+    // precision escalation: pixels whose rebases cancelled more than
+    // lost_limit bits are appended to flag_out (frame-linear indices)
+    float lost_limit = 1e30f;
+    unsigned* flag_out = nullptr;
+    unsigned* flag_out_count = nullptr;
+    const unsigned* list_in = nullptr;        // list pass: pixels to render
+    const unsigned* list_in_count = nullptr;
 };
-int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s);
+// pass 0: FP32 frame pass; pass 1: FP64 pass over list_in
+int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass);
 
 // Fixed-point conversion helpers (host).  A fixed-point number has `words`
 // 32-bit words, two's complement, least significant first, and

@@ -103,7 +103,8 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
     const int lane = threadIdx.x & 31;
     const int tiles_x = (p.W + kTileW - 1) / kTileW;
     const int tiles_y = (p.nrows + kTileH - 1) / kTileH;
-    const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y;
+    const unsigned list_n = p.list ? *p.list_count : 0u;
+    const unsigned total = p.list ? (list_n + 31u) / 32u : (unsigned)tiles_x * (unsigned)tiles_y;
     for (;;) {
         unsigned tile = 0;
         if (lane == 0)
@@ -111,12 +112,23 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
         tile = __shfl_sync(0xffffffffu, tile, 0);
         if (tile >= total)
             break;
-        const int ty = (int)(tile / (unsigned)tiles_x);
-        const int tx = (int)(tile - (unsigned)ty * (unsigned)tiles_x);
-        const int ix = tx * kTileW + (lane & (kTileW - 1));
-        const int lrow = ty * kTileH + (lane / kTileW);
+        int ix, lrow, ty = 0;
+        bool valid;
+        if (p.list) {
+            const unsigned i = tile * 32u + lane;
+            valid = i < list_n;
+            const unsigned pix = valid ? p.list[i] : 0u;
+            lrow = (int)(pix / (unsigned)p.W);
+            ix = (int)(pix - (unsigned)lrow * (unsigned)p.W);
+        } else {
+            ty = (int)(tile / (unsigned)tiles_x);
+            const int tx = (int)(tile - (unsigned)ty * (unsigned)tiles_x);
+            ix = tx * kTileW + (lane & (kTileW - 1));
+            lrow = ty * kTileH + (lane / kTileW);
+            valid = ix < p.W && lrow < p.nrows;
+        }
         unsigned long long its = 0;
-        if (ix < p.W && lrow < p.nrows) {
+        if (valid) {
             uint32_t wre[N], wim[N];
             const uint32_t* xs = p.xs + (size_t)ix * N;
             const uint32_t* ys = p.ys + (size_t)lrow * N;
@@ -155,7 +167,7 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
         __syncwarp();
         if (lane == 0) {
             atomicAdd(&p.sync->iter_sum, its);
-            if (p.tile_rows_done) {
+            if (p.tile_rows_done && !p.list) {
                 const unsigned done = atomicAdd(&p.tile_rows_done[ty], 1u) + 1u;
                 if (done == (unsigned)tiles_x && p.band_flags) {
                     __threadfence_system();
@@ -182,7 +194,8 @@ int launch_typed(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
         if (blocks_per_sm < 1)
             blocks_per_sm = 1;
     }
-    const long tiles = (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
+    const long tiles = p.list ? ((long)p.W * p.nrows + 31) / 32
+                              : (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
     long grid = (long)ctx->num_sms * blocks_per_sm;
     const long blocks_needed = (tiles + threads / 32 - 1) / (threads / 32);
     if (grid > blocks_needed)

@@ -255,41 +255,73 @@ __global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
 // Pixels
 // --------------------------------------------------------------------------
 
+// Mantissa traits of the pixel loop: FP32 (the fast pass) or FP64 (the
+// escalation pass for pixels whose rebases cancelled too many bits).
+template <class T>
+struct Mant;
+template <>
+struct Mant<float> {
+    static constexpr int kMinExp = -149;     // below: 2^e is 0
+    static constexpr int kSlowExp = -120;    // dz^2 term may vanish below
+    static constexpr int kSqExp = -63;       // 2^(2e) representable above
+    static constexpr float kTinyZ2 = 7.5e-37f;   // |Z|^2 < 2^-120
+    static constexpr float kGlitchZ2 = 8.7e-19f; // |Z|^2 < 2^-60
+    static constexpr int kForceSlow = 120;   // dc 2^-e would overflow above
+    __device__ static float scale(float x, int e) { return ldexpf(x, e); }
+    __device__ static float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+    __device__ static int exponent_of(float a) { return ((__float_as_int(a) >> 23) & 0xff) - 127; }
+};
+template <>
+struct Mant<double> {
+    static constexpr int kMinExp = -1074;
+    static constexpr int kSlowExp = -1000;
+    static constexpr int kSqExp = -511;
+    static constexpr double kTinyZ2 = 1e-300;
+    static constexpr double kGlitchZ2 = 8.7e-19;
+    static constexpr int kForceSlow = 1000;
+    __device__ static double scale(double x, int e) { return ldexp(x, e); }
+    __device__ static double fma_(double a, double b, double c) { return fma(a, b, c); }
+    __device__ static int exponent_of(double a) { return ilogb(a); }
+};
+
+template <class T>
 struct PixState {
-    float tr, ti;   // dz mantissas
+    T tr, ti;       // dz mantissas
     int e;          // dz = t * 2^e
-    float s;        // 2^e (0 below the FP32 range)
-    float s2x4;     // 4 * 2^(2e), 0 when e < -63
-    float dcr, dci; // dc * 2^-e
+    T s;            // 2^e (0 below the range)
+    T s2x4;         // 4 * 2^(2e), 0 when 2^(2e) underflows
+    T dcr, dci;     // dc * 2^-e
     bool slow_if_tiny;
     bool force_slow;
 };
 
-__device__ __forceinline__ void refresh_scale(PixState& st, float dcm_r, float dcm_i, int dce)
+template <class T>
+__device__ __forceinline__ void refresh_scale(PixState<T>& st, T dcm_r, T dcm_i, int dce)
 {
-    st.s = ldexpf(1.0f, st.e);
-    st.s2x4 = st.e >= -63 ? 4.0f * st.s * st.s : 0.0f;
-    st.dcr = ldexpf(dcm_r, dce - st.e);
-    st.dci = ldexpf(dcm_i, dce - st.e);
-    st.slow_if_tiny = st.e < -120;
-    // dc * 2^-e would overflow FP32 (dz far below dc); a pixel with dc == 0
+    st.s = Mant<T>::scale((T)1, st.e);
+    st.s2x4 = st.e >= Mant<T>::kSqExp ? (T)4 * st.s * st.s : (T)0;
+    st.dcr = Mant<T>::scale(dcm_r, dce - st.e);
+    st.dci = Mant<T>::scale(dcm_i, dce - st.e);
+    st.slow_if_tiny = st.e < Mant<T>::kSlowExp;
+    // dc * 2^-e would overflow (dz far below dc); a pixel with dc == 0
     // is the reference point itself and never needs it.
-    st.force_slow = (dcm_r != 0.f || dcm_i != 0.f) && (dce - st.e) > 120;
+    st.force_slow = (dcm_r != (T)0 || dcm_i != (T)0) && (dce - st.e) > Mant<T>::kForceSlow;
 }
 
 // Set t, e from a double pair scaled by 2^E.
-__device__ __forceinline__ void set_from_double(PixState& st, double xr, double xi, int E)
+template <class T>
+__device__ __forceinline__ void set_from_double(PixState<T>& st, double xr, double xi, int E)
 {
     const double a = fmax(fabs(xr), fabs(xi));
     if (a == 0.0) {
-        st.tr = 0.f;
-        st.ti = 0.f;
+        st.tr = (T)0;
+        st.ti = (T)0;
         st.e = E;
         return;
     }
     const int k = ilogb(a);
-    st.tr = (float)ldexp(xr, -k);
-    st.ti = (float)ldexp(xi, -k);
+    st.tr = (T)ldexp(xr, -k);
+    st.ti = (T)ldexp(xi, -k);
     st.e = E + k;
 }
 
@@ -298,17 +330,29 @@ __device__ __forceinline__ int dexp_of(double x)
     return x == 0.0 ? -100000 : ilogb(x);
 }
 
-template <bool WANT_MAG>
+// One pixel.  Returns the count; mag_out gets |z|^2 at escape.  `lost`
+// accumulates the bits cancelled by rebases (log2 |dz| / |z| at each one):
+// a pixel whose deltas lost more than the mantissa can spare is re-run by
+// the next, more precise, pass.
+template <class T>
 __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
-                                  float& mag_out, unsigned& rebases)
+                                  float& mag_out, unsigned& rebases, float& lost)
 {
-    const float dcf_r = (float)dcm_r, dcf_i = (float)dcm_i;
-    PixState st;
+    const T dcf_r = (T)dcm_r, dcf_i = (T)dcm_i;
+    PixState<T> st;
     set_from_double(st, dcm_r, dcm_i, dce);
     refresh_scale(st, dcf_r, dcf_i, dce);
     int m = 1;
     const int K = *p.orbit_len;  // entries 0..K-1 valid
-    float2 Z = p.zf[1];
+    float2 Zf = p.zf[1];
+    T Zx = (T)Zf.x, Zy = (T)Zf.y;
+    if (sizeof(T) == 8) {
+        const double2 zd = p.zd[1];
+        if (p.ze[1] == 0) {
+            Zx = (T)zd.x;
+            Zy = (T)zd.y;
+        }
+    }
     float mag = 0.f;
     for (uint32_t wz = 1; wz <= p.depth; ++wz) {
         if (m >= K - 1) {
@@ -316,24 +360,27 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
             const double2 zd = p.zd[m];
             const int ze = p.ze[m];
             const int E = max(dexp_of(fmax(fabs(zd.x), fabs(zd.y))) + ze, st.e + 40);
-            const double zr = ldexp(zd.x, ze - E) + ldexp((double)st.tr, st.e - E);
-            const double zi = ldexp(zd.y, ze - E) + ldexp((double)st.ti, st.e - E);
+            const double dr = ldexp((double)st.tr, st.e - E), di = ldexp((double)st.ti, st.e - E);
+            const double zr = ldexp(zd.x, ze - E) + dr;
+            const double zi = ldexp(zd.y, ze - E) + di;
+            const double z2 = zr * zr + zi * zi, d2 = dr * dr + di * di;
+            if (d2 > z2 && z2 > 0.0)
+                lost += 0.5f * (float)log2(d2 / z2);
             set_from_double(st, zr, zi, E);
             refresh_scale(st, dcf_r, dcf_i, dce);
             m = 0;
-            Z = p.zf[0];
+            Zx = (T)0;
+            Zy = (T)0;
             ++rebases;
         }
-        const float zm2 = Z.x * Z.x + Z.y * Z.y;
-        if (st.force_slow || (st.slow_if_tiny && zm2 < 7.5e-37f /* 2^-120 */)) {
+        const T zm2 = Zx * Zx + Zy * Zy;
+        if (st.force_slow || (st.slow_if_tiny && zm2 < (T)Mant<T>::kTinyZ2)) {
             // full floatexp step in FP64: dz' = 2 Z dz + dz^2 + dc
             const double2 zd = p.zd[m];
             const int ze = p.ze[m];
-            const double tr = st.tr, ti = st.ti;
-            // A = 2 Z t  * 2^(ze + e)
+            const double tr = (double)st.tr, ti = (double)st.ti;
             const double ar = 2.0 * (zd.x * tr - zd.y * ti), ai = 2.0 * (zd.x * ti + zd.y * tr);
             const int ae = ze + st.e;
-            // B = t^2 * 2^(2e)
             const double br = tr * tr - ti * ti, bi = 2.0 * tr * ti;
             const int be = 2 * st.e;
             const int E = max(max(dexp_of(fmax(fabs(ar), fabs(ai))) + ae,
@@ -344,20 +391,30 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
             set_from_double(st, rr, ri, E);
             refresh_scale(st, dcf_r, dcf_i, dce);
         } else {
-            const float tr = st.tr, ti = st.ti;
-            const float u = tr + tr, v = ti + ti;
-            const float a = fmaf(tr, tr, -ti * ti);  // t^2 real
-            const float b = tr * v;                  // t^2 imag
-            st.tr = fmaf(Z.x, u, fmaf(-Z.y, v, fmaf(st.s, a, st.dcr)));
-            st.ti = fmaf(Z.x, v, fmaf(Z.y, u, fmaf(st.s, b, st.dci)));
+            const T tr = st.tr, ti = st.ti;
+            const T u = tr + tr, v = ti + ti;
+            const T a = Mant<T>::fma_(tr, tr, -ti * ti);  // t^2 real
+            const T b = tr * v;                           // t^2 imag
+            st.tr = Mant<T>::fma_(Zx, u, Mant<T>::fma_(-Zy, v, Mant<T>::fma_(st.s, a, st.dcr)));
+            st.ti = Mant<T>::fma_(Zx, v, Mant<T>::fma_(Zy, u, Mant<T>::fma_(st.s, b, st.dci)));
         }
         ++m;
-        Z = p.zf[m];
-        const float zr = fmaf(st.s, st.tr, Z.x);
-        const float zi = fmaf(st.s, st.ti, Z.y);
-        mag = fmaf(zr, zr, zi * zi);
-        bool esc = mag > 4.0f;
-        if (fabsf(mag - 4.0f) < 6.1035156e-5f /* 2^-14 */) {
+        if (sizeof(T) == 4) {
+            Zf = p.zf[m];
+            Zx = (T)Zf.x;
+            Zy = (T)Zf.y;
+        } else {
+            const double2 zd = p.zd[m];
+            const int ze = p.ze[m];
+            Zx = (T)(ze ? ldexp(zd.x, ze) : zd.x);
+            Zy = (T)(ze ? ldexp(zd.y, ze) : zd.y);
+        }
+        const T zr = Mant<T>::fma_(st.s, st.tr, Zx);
+        const T zi = Mant<T>::fma_(st.s, st.ti, Zy);
+        const T magT = Mant<T>::fma_(zr, zr, zi * zi);
+        mag = (float)magT;
+        bool esc = magT > (T)4;
+        if (fabs((double)magT - 4.0) < 6.1035156e-5 /* 2^-14 */) {
             // |z|^2 - 4 = D_m + 2 Re(conj(Z_m) dz) + |dz|^2, in FP64 with
             // explicit exponents (D_m exact from the orbit digits)
             const double2 zd = p.zd[m];
@@ -376,9 +433,10 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
             mag_out = mag;
             return wz;
         }
-        const float dd = fmaf(st.tr, st.tr, st.ti * st.ti);
-        const float zn2 = fmaf(Z.x, Z.x, Z.y * Z.y);
-        const bool maybe = st.e >= -63 ? (st.s2x4 * dd >= zn2) : (zn2 < 8.7e-19f /* 2^-60 */);
+        const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
+        const T zn2 = Mant<T>::fma_(Zx, Zx, Zy * Zy);
+        const bool maybe =
+            st.e >= Mant<T>::kSqExp ? (st.s2x4 * dd >= zn2) : (zn2 < (T)Mant<T>::kGlitchZ2);
         if (maybe) {
             // rebase test |Z_m + dz| < |dz| in FP64
             const double2 zd = p.zd[m];
@@ -386,19 +444,23 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
             const int E = max(dexp_of(fmax(fabs(zd.x), fabs(zd.y))) + ze, st.e + 40);
             const double dr = ldexp((double)st.tr, st.e - E), di = ldexp((double)st.ti, st.e - E);
             const double fr = ldexp(zd.x, ze - E) + dr, fi = ldexp(zd.y, ze - E) + di;
-            if (fr * fr + fi * fi < dr * dr + di * di) {
+            const double z2 = fr * fr + fi * fi, d2 = dr * dr + di * di;
+            if (z2 < d2) {
+                if (z2 > 0.0)
+                    lost += 0.5f * (float)log2(d2 / z2);
                 set_from_double(st, fr, fi, E);
                 refresh_scale(st, dcf_r, dcf_i, dce);
                 m = 0;
-                Z = p.zf[0];
+                Zx = (T)0;
+                Zy = (T)0;
                 ++rebases;
                 continue;
             }
         }
-        const float amax = fmaxf(fabsf(st.tr), fabsf(st.ti));
-        if ((amax > 4.2949673e9f || amax < 2.3283064e-10f) && amax != 0.0f) {
-            const int k = ((__float_as_int(amax) >> 23) & 0xff) - 127;
-            const float sc = ldexpf(1.0f, -k);
+        const T amax = fmax(fabs(st.tr), fabs(st.ti));
+        if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
+            const int k = Mant<T>::exponent_of(amax);
+            const T sc = Mant<T>::scale((T)1, -k);
             st.tr *= sc;
             st.ti *= sc;
             st.e += k;
@@ -417,13 +479,19 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
-template <bool WANT_MAG>
-__global__ void __launch_bounds__(256) perturb_frame_kernel(PerturbLaunch p)
+// Frame pass (FP32): 8x4 tiles per warp from the atomic counter.  Pass 2
+// (FP64) walks the list of pixels the previous pass flagged, in warp-sized
+// chunks.  Each pass appends the pixels it could not finish precisely to
+// p.flag_out; pixel-iterations are counted only for pixels it finalises.
+template <class T, bool WANT_MAG, bool LIST>
+__global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
 {
     const int lane = threadIdx.x & 31;
     const int tiles_x = (p.W + kTileW - 1) / kTileW;
     const int tiles_y = (p.nrows + kTileH - 1) / kTileH;
-    const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y;
+    const unsigned total = LIST ? (unsigned)((*p.list_in_count + 31) / 32)
+                                : (unsigned)tiles_x * (unsigned)tiles_y;
+    const unsigned list_n = LIST ? *p.list_in_count : 0u;
     for (;;) {
         unsigned tile = 0;
         if (lane == 0)
@@ -431,24 +499,40 @@ __global__ void __launch_bounds__(256) perturb_frame_kernel(PerturbLaunch p)
         tile = __shfl_sync(0xffffffffu, tile, 0);
         if (tile >= total)
             break;
-        const int ty = (int)(tile / (unsigned)tiles_x);
-        const int tx = (int)(tile - (unsigned)ty * (unsigned)tiles_x);
-        const int ix = tx * kTileW + (lane & (kTileW - 1));
-        const int lrow = ty * kTileH + (lane / kTileW);
+        int ix, lrow;
+        bool valid;
+        if (LIST) {
+            const unsigned i = tile * 32u + lane;
+            valid = i < list_n;
+            const unsigned pix = valid ? p.list_in[i] : 0u;
+            lrow = (int)(pix / (unsigned)p.W);
+            ix = (int)(pix - (unsigned)lrow * (unsigned)p.W);
+        } else {
+            const int ty = (int)(tile / (unsigned)tiles_x);
+            const int tx = (int)(tile - (unsigned)ty * (unsigned)tiles_x);
+            ix = tx * kTileW + (lane & (kTileW - 1));
+            lrow = ty * kTileH + (lane / kTileW);
+            valid = ix < p.W && lrow < p.nrows;
+        }
         unsigned long long its = 0;
         unsigned reb = 0;
-        if (ix < p.W && lrow < p.nrows) {
+        if (valid) {
             const int line = p.row0 + lrow;
             // dc = ((2 ix - W) hs, (H - 2 line) hs), hs = half pixel spacing
             const double dcm_r = (double)(2 * ix - p.W) * p.hs_m;
             const double dcm_i = (double)(p.H - 2 * line) * p.hs_m;
-            float mag = 0.f;
-            const uint32_t n = perturb_pixel<WANT_MAG>(p, dcm_r, dcm_i, p.hs_e, mag, reb);
+            float mag = 0.f, lost = 0.f;
+            const uint32_t n = perturb_pixel<T>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost);
             const size_t o = (size_t)lrow * p.W + ix;
             p.out[o] = (int32_t)n;
             if (WANT_MAG)
                 p.mag[o] = mag;
-            its = n ? n : p.depth;
+            if (lost > p.lost_limit && p.flag_out) {
+                const unsigned slot = atomicAdd(p.flag_out_count, 1u);
+                p.flag_out[slot] = (unsigned)o;
+            } else {
+                its = n ? n : p.depth;
+            }
         }
         its = warp_sum_u64(its);
         unsigned long long rb = warp_sum_u64((unsigned long long)reb);
@@ -476,29 +560,39 @@ int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
     return MDZGPU_OK;
 }
 
-int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s)
+template <class T, bool WANT_MAG, bool LIST>
+int launch_pass(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
 {
-    static int bps[2] = {0, 0};
-    const int w = p.mag ? 1 : 0;
-    if (!bps[w]) {
+    static int bps = 0;
+    if (!bps) {
         MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &bps[w], w ? perturb_frame_kernel<true> : perturb_frame_kernel<false>, 256, 0));
-        if (bps[w] < 1)
-            bps[w] = 1;
+            &bps, perturb_kernel<T, WANT_MAG, LIST>, 256, 0));
+        if (bps < 1)
+            bps = 1;
     }
-    const long tiles = (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
-    long grid = (long)ctx->num_sms * bps[w];
-    const long blocks_needed = (tiles + 7) / 8;
+    long grid = (long)ctx->num_sms * bps;
+    const long blocks_needed = (work_items + 7) / 8;
     if (grid > blocks_needed)
         grid = blocks_needed;
     if (grid < 1)
         grid = 1;
-    if (w)
-        perturb_frame_kernel<true><<<(unsigned)grid, 256, 0, s>>>(p);
-    else
-        perturb_frame_kernel<false><<<(unsigned)grid, 256, 0, s>>>(p);
+    perturb_kernel<T, WANT_MAG, LIST><<<(unsigned)grid, 256, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
     return MDZGPU_OK;
+}
+
+int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass)
+{
+    const bool mag = p.mag != nullptr;
+    if (pass == 0) {
+        const long tiles = (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
+        return mag ? launch_pass<float, true, false>(ctx, p, s, tiles)
+                   : launch_pass<float, false, false>(ctx, p, s, tiles);
+    }
+    // list pass: sized for the worst case, exits at once on an empty list
+    const long chunks = ((long)p.W * p.nrows + 31) / 32;
+    return mag ? launch_pass<double, true, true>(ctx, p, s, chunks)
+               : launch_pass<double, false, true>(ctx, p, s, chunks);
 }
 
 int orbit_max_limbs()

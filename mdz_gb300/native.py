@@ -27,7 +27,8 @@ class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("wall_ms", C.c_double),
                 ("pixel_iters", C.c_int64), ("h2d_bytes", C.c_int64),
                 ("d2h_bytes", C.c_int64), ("launches", C.c_int32), ("words", C.c_int32),
-                ("orbit_ms", C.c_double), ("rebases", C.c_int64), ("orbit_len", C.c_int64)]
+                ("orbit_ms", C.c_double), ("rebases", C.c_int64), ("orbit_len", C.c_int64),
+                ("escalated_fp64", C.c_int64), ("escalated_mp", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -331,6 +331,8 @@ typedef struct {
     long prec;
     const char* const* cre;
     const char* const* cim;
+    const char* jre;  /* Julia family: fixed c (z0 = the listed point) */
+    const char* jim;
     int64_t* counts;
     double* mag2;
     int next;
@@ -356,10 +358,15 @@ static void* points_worker(void* arg)
         pthread_mutex_unlock(&j->mu);
         if (i >= j->n)
             break;
-        mpfr_set_str(c_re, j->cre[i], 0, GMP_RNDN);
-        mpfr_set_str(c_im, j->cim[i], 0, GMP_RNDN);
-        mpfr_set(wre, c_re, GMP_RNDN);
-        mpfr_set(wim, c_im, GMP_RNDN);
+        mpfr_set_str(wre, j->cre[i], 0, GMP_RNDN);
+        mpfr_set_str(wim, j->cim[i], 0, GMP_RNDN);
+        if (j->jre) {
+            mpfr_set_str(c_re, j->jre, 0, GMP_RNDN);
+            mpfr_set_str(c_im, j->jim, 0, GMP_RNDN);
+        } else {
+            mpfr_set(c_re, wre, GMP_RNDN);
+            mpfr_set(c_im, wim, GMP_RNDN);
+        }
         mpfr_mul(wre2, wre, wre, GMP_RNDN);
         mpfr_mul(wim2, wim, wim, GMP_RNDN);
         double m2 = 0.0;
@@ -382,11 +389,26 @@ static void* points_worker(void* arg)
 
 /* n Mandelbrot-family pixels c_i (strings, parsed at `prec` bits) through the
  * MPFR loop; counts[i] and |z|^2 at escape (mag2, nullable). */
+int mdzo_points_julia_mpfr(int n, int fractal, int64_t depth, long prec,
+                           const char* const* zre, const char* const* zim, const char* jre,
+                           const char* jim, int nthreads, int64_t* counts, double* mag2);
+
 int mdzo_points_mpfr(int n, int fractal, int64_t depth, long prec, const char* const* cre,
                      const char* const* cim, int nthreads, int64_t* counts, double* mag2)
 {
+    return mdzo_points_julia_mpfr(n, fractal, depth, prec, cre, cim, 0, 0, nthreads, counts,
+                                  mag2);
+}
+
+/* Julia family (jre != NULL): z0 = the listed points, c = (jre, jim). */
+int mdzo_points_julia_mpfr(int n, int fractal, int64_t depth, long prec,
+                           const char* const* cre, const char* const* cim, const char* jre,
+                           const char* jim, int nthreads, int64_t* counts, double* mag2)
+{
     points_job j;
     memset(&j, 0, sizeof j);
+    j.jre = jre;
+    j.jim = jim;
     j.n = n;
     j.fractal = fractal;
     j.depth = depth;

@@ -43,6 +43,11 @@ def lib() -> C.CDLL:
             L.mdzo_points_mpfr.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_long,
                                            C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
                                            C.c_int, C.c_void_p, C.c_void_p]
+            L.mdzo_points_julia_mpfr.restype = C.c_int
+            L.mdzo_points_julia_mpfr.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_long,
+                                                 C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
+                                                 C.c_char_p, C.c_char_p, C.c_int, C.c_void_p,
+                                                 C.c_void_p]
         _orc = L
     return _orc
 
@@ -84,6 +89,17 @@ def points_mpfr(cre: list[str], cim: list[str], depth: int, prec: int, fractal=0
     lib().mdzo_points_mpfr(n, fractal, depth, prec, a, b, threads, counts.ctypes.data,
                            mag.ctypes.data)
     return counts, mag
+
+
+def points_julia_mpfr(zre, zim, jre: str, jim: str, depth, prec, fractal=0, threads=1):
+    """Julia family: z0 = the listed points, c = (jre, jim)."""
+    n = len(zre)
+    a = (C.c_char_p * n)(*[s.encode() for s in zre])
+    b = (C.c_char_p * n)(*[s.encode() for s in zim])
+    counts = np.empty(n, np.int64)
+    lib().mdzo_points_julia_mpfr(n, fractal, depth, prec, a, b, jre.encode(), jim.encode(),
+                                 threads, counts.ctypes.data, None)
+    return counts
 
 
 # ---- the unmodified reference (only where it was compiled) ----

@@ -187,11 +187,17 @@ def make_views() -> None:
 # Multiprecision fixtures (reference MPFR path at p and 2p)
 # --------------------------------------------------------------------------
 
+_RECTS: dict = {}
+
+
 def mdz_mpfr_c(v: View, prec: int, ix: int, line: int) -> tuple[Fraction, Fraction]:
     """c of pixel (ix, line) exactly as fractal_mpfr_calculate_line computes
     it at `prec` bits (src/fractal.c:159-186) from image_info's rect."""
     from mdz_gb300.views import mdz_rect
-    r = mdz_rect(v.width, v.height, prec, v.cx, v.cy, v.size)
+    key = (v.width, v.height, v.precision, v.cx, v.cy, v.size)
+    if key not in _RECTS:
+        _RECTS[key] = mdz_rect(*key)
+    r = _RECTS[key]
 
     def rn(x):
         return MpVal.from_fraction(x, prec).to_fraction()
@@ -269,16 +275,37 @@ def mp_views() -> list[View]:
 
 
 def make_mp() -> None:
+    """Counts of the reference's MPFR path at the view's precision p, and the
+    arbiter: the same pixel c values (p-bit, as fractal_mpfr_calculate_line
+    rounds them) iterated with MPFR at 2p."""
     out, meta = {}, {}
     for v in mp_views():
         t0 = time.time()
         ref, _ = O.ref_render(v, threads=THREADS)
-        v2 = View.from_dict(dict(v.__dict__, precision=2 * v.precision))
-        ref2, _ = O.ref_render(v2, threads=THREADS)
+        cre, cim = [], []
+        for ln in range(v.real_height):
+            for ix in range(v.real_width):
+                x, y = mdz_mpfr_c(v, v.precision, ix, ln)
+                cre.append(hexfloat(x))
+                cim.append(hexfloat(y))
+        if v.family:
+            jre, jim = (x.to_fraction() for x in v.julia())
+            p1 = O.points_julia_mpfr(cre, cim, hexfloat(jre), hexfloat(jim), v.depth,
+                                     v.precision, v.fractal, THREADS)
+            p2 = O.points_julia_mpfr(cre, cim, hexfloat(jre), hexfloat(jim), v.depth,
+                                     2 * v.precision, v.fractal, THREADS)
+        else:
+            p1, _ = O.points_mpfr(cre, cim, v.depth, v.precision, fractal=v.fractal,
+                                  threads=THREADS)
+            p2, _ = O.points_mpfr(cre, cim, v.depth, 2 * v.precision, fractal=v.fractal,
+                                  threads=THREADS)
+        p1 = p1.reshape(ref.shape).astype(np.int32)
+        p2 = p2.reshape(ref.shape).astype(np.int32)
+        assert np.array_equal(p1, ref), f"{v.name}: pixel c restatement differs from reference"
         out[v.name] = ref
-        out[v.name + "__2p"] = ref2
+        out[v.name + "__2p"] = p2
         meta[v.name] = dict(v.__dict__)
-        print(f"{v.name}: confirmed {(ref == ref2).mean():.4f} "
+        print(f"{v.name}: confirmed {(ref == p2).mean():.4f} "
               f"iters={pixel_iters(ref, v.depth)} ({time.time() - t0:.1f}s)")
     # config 3 (640x480, 256 bits, width 2^-200, maxiter 50000) on a
     # subsampled pixel grid: every 8th column and row, at p and 2p
@@ -286,14 +313,14 @@ def make_mp() -> None:
     step = 8
     ixs = list(range(0, c3.real_width, step))
     lns = list(range(0, c3.real_height, step))
+    cre, cim = [], []
+    for ln in lns:
+        for ix in ixs:
+            x, y = mdz_mpfr_c(c3, c3.precision, ix, ln)
+            cre.append(hexfloat(x))
+            cim.append(hexfloat(y))
     for prec, key in ((c3.precision, "c3_sub"), (2 * c3.precision, "c3_sub__2p")):
         t0 = time.time()
-        cre, cim = [], []
-        for ln in lns:
-            for ix in ixs:
-                x, y = mdz_mpfr_c(c3, prec, ix, ln)
-                cre.append(hexfloat(x))
-                cim.append(hexfloat(y))
         counts, _ = O.points_mpfr(cre, cim, c3.depth, prec, threads=THREADS)
         out[key] = counts.reshape(len(lns), len(ixs)).astype(np.int32)
         print(f"{key}: {time.time() - t0:.1f}s")
