@@ -198,6 +198,18 @@ int mdzgpu_render_perturb_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
  * with hs_m in [1, 2) holding at most 40 significant bits. */
 int mdzgpu_perturb_spacing(const mdzgpu_mpval* width, int32_t W,
                            double* hs_m, int32_t* hs_e);
+/* The reference orbit alone: Z_0 = 0, Z_1 = C, Z_{k+1} = Z_k^2 + C for the
+ * centre (cx, cy), iterated on the GPU in `limbs` radix-2^28 digits until
+ * |Z_k| > 2 or k = max_k.  Writes *len entries (arrays hold max_k + 1):
+ * z_re/z_im = Z_k rounded to double (ldexp-scaled, may underflow), and
+ * D_k = |Z_k|^2 - 4 = d_mant * 2^d_exp (exact from the digits when
+ * |D_k| < 2^-20).  Any output pointer may be NULL. */
+int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx,
+                           const mdzgpu_mpval* cy, int64_t precision,
+                           int32_t limbs, int64_t max_k, double* z_re,
+                           double* z_im, double* d_mant, int32_t* d_exp,
+                           int64_t* len);
+
 /* Orbit digits chosen for a precision (ceil(precision / 28) + 1, >= 5). */
 int32_t mdzgpu_perturb_limbs(int64_t precision);
 

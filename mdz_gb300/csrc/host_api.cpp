@@ -529,8 +529,8 @@ int32_t mdzgpu_perturb_limbs(int64_t precision)
 
 // Bits a pass may lose to rebase cancellation before its pixel is re-run by
 // the next, more precise pass (FP32 -> FP64 -> multi-limb).
-constexpr float kLostLimitFp32 = 4.0f;
-constexpr float kLostLimitFp64 = 20.0f;
+constexpr float kLostLimitFp32 = 2.0f;
+constexpr float kLostLimitFp64 = 10.0f;
 
 // Fixed-point pixel coordinates of the perturbation geometry for the
 // multi-limb pass: x[ix] = cx + (2 ix - W) hs, y[line] = cy + (H - 2 line) hs.
@@ -784,6 +784,80 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     }
     cudaEventDestroy(evo);
     return rc;
+}
+
+int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx, const mdzgpu_mpval* cy,
+                           int64_t precision, int32_t limbs, int64_t max_k, double* z_re,
+                           double* z_im, double* d_mant, int32_t* d_exp, int64_t* len)
+{
+    if (!ctx || max_k < 1 || max_k > 0x7ffffffeLL) {
+        set_error("reference orbit: bad arguments");
+        return MDZGPU_ERR_ARG;
+    }
+    MDZ_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int L = limbs > 0 ? limbs : mdzgpu_perturb_limbs(precision);
+    if (L > orbit_max_limbs() || L < 5) {
+        set_error("reference orbit: %d limbs outside [5, %d]", L, orbit_max_limbs());
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    std::vector<int> dig(2 * (size_t)L);
+    if (digits28_from_mpval(cx, L, dig.data()) || digits28_from_mpval(cy, L, dig.data() + L)) {
+        set_error("reference orbit: centre outside the fixed-point range");
+        return MDZGPU_ERR_RANGE;
+    }
+    const size_t entries = (size_t)max_k + 1;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t off_zd = al(entries * sizeof(float2));
+    const size_t off_ze = off_zd + al(entries * sizeof(double2));
+    const size_t off_dd = off_ze + al(entries * sizeof(int));
+    const size_t off_de = off_dd + al(entries * sizeof(double));
+    const size_t off_len = off_de + al(entries * sizeof(int));
+    const size_t off_dig = off_len + 256;
+    const size_t off_raw = off_dig + al(2 * L * sizeof(int));
+    const size_t bytes = off_raw + al(entries * 2 * (size_t)L * sizeof(int));
+    int rc = ctx->orbit.ensure(bytes);
+    if (rc)
+        return rc;
+    char* ob = (char*)ctx->orbit.ptr;
+    MDZ_CUDA_TRY(cudaMemcpyAsync(ob + off_dig, dig.data(), dig.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    OrbitLaunch o;
+    o.limbs = L;
+    o.c_re = (const int*)(ob + off_dig);
+    o.c_im = o.c_re + L;
+    o.zf = (float2*)ob;
+    o.zd = (double2*)(ob + off_zd);
+    o.ze = (int*)(ob + off_ze);
+    o.dd = (double*)(ob + off_dd);
+    o.de = (int*)(ob + off_de);
+    o.digits = (int*)(ob + off_raw);
+    o.max_k = (int)max_k;
+    o.out_len = (int*)(ob + off_len);
+    if ((rc = launch_orbit(o, ctx->stream)))
+        return rc;
+    int n = 0;
+    MDZ_CUDA_TRY(cudaMemcpyAsync(&n, o.out_len, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    MDZ_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    std::vector<double2> zd(n);
+    std::vector<int> ze(n), de(n);
+    std::vector<double> dd(n);
+    MDZ_CUDA_TRY(cudaMemcpy(zd.data(), o.zd, n * sizeof(double2), cudaMemcpyDeviceToHost));
+    MDZ_CUDA_TRY(cudaMemcpy(ze.data(), o.ze, n * sizeof(int), cudaMemcpyDeviceToHost));
+    MDZ_CUDA_TRY(cudaMemcpy(dd.data(), o.dd, n * sizeof(double), cudaMemcpyDeviceToHost));
+    MDZ_CUDA_TRY(cudaMemcpy(de.data(), o.de, n * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n; ++k) {
+        if (z_re)
+            z_re[k] = ldexp(zd[k].x, ze[k]);
+        if (z_im)
+            z_im[k] = ldexp(zd[k].y, ze[k]);
+        if (d_mant)
+            d_mant[k] = dd[k];
+        if (d_exp)
+            d_exp[k] = de[k];
+    }
+    if (len)
+        *len = n;
+    return MDZGPU_OK;
 }
 
 int mdzgpu_render_perturb(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,

@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
     __syncwarp();
     const int cbase = L - 4;       // lowest column computed (3 guard columns)
     const int ctop = 2 * L - 2;    // highest column
+    const int nslots = (ctop - cbase + 32) / 32;
     int k = 1;
     for (;; ++k) {
         // escape test on the two top digits (FP32 is enough to stop the
@@ -109,23 +110,40 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
         escaped = __shfl_sync(0xffffffffu, escaped, 0);
         if (escaped || k >= p.max_k)
             break;
-        long long vr[3], vi[3];
+        long long vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
-            vr[s] = 0;
-            vi[s] = 0;
             const int c = cbase + lane + 32 * s;
-            if (c > ctop)
+            if (s >= nslots || c > ctop)
                 continue;
             const int ilo = c - (L - 1) > 0 ? c - (L - 1) : 0;
             const int ihi = (c - 1) >> 1;  // i < j = c - i
-            long long pr = 0, pi = 0;
-            for (int i = ilo; i <= ihi; ++i) {
+            // four independent accumulator pairs: the pair loop is bound by
+            // shared-memory and IMAD latency, not throughput
+            long long pr0 = 0, pi0 = 0, pr1 = 0, pi1 = 0, pr2 = 0, pi2 = 0, pr3 = 0, pi3 = 0;
+            int i = ilo;
+            for (; i + 3 <= ihi; i += 4) {
+                const int j = c - i;
+                const long long a0 = zr[i], b0 = zi[i], c0 = zr[j], d0 = zi[j];
+                const long long a1 = zr[i + 1], b1 = zi[i + 1], c1 = zr[j - 1], d1 = zi[j - 1];
+                const long long a2 = zr[i + 2], b2 = zi[i + 2], c2 = zr[j - 2], d2 = zi[j - 2];
+                const long long a3 = zr[i + 3], b3 = zi[i + 3], c3 = zr[j - 3], d3 = zi[j - 3];
+                pr0 += a0 * c0 - b0 * d0;
+                pi0 += a0 * d0 + c0 * b0;
+                pr1 += a1 * c1 - b1 * d1;
+                pi1 += a1 * d1 + c1 * b1;
+                pr2 += a2 * c2 - b2 * d2;
+                pi2 += a2 * d2 + c2 * b2;
+                pr3 += a3 * c3 - b3 * d3;
+                pi3 += a3 * d3 + c3 * b3;
+            }
+            for (; i <= ihi; ++i) {
                 const int j = c - i;
                 const long long ari = zr[i], aii = zi[i], arj = zr[j], aij = zi[j];
-                pr += ari * arj - aii * aij;
-                pi += ari * aij + arj * aii;
+                pr0 += ari * arj - aii * aij;
+                pi0 += ari * aij + arj * aii;
             }
+            const long long pr = (pr0 + pr1) + (pr2 + pr3), pi = (pi0 + pi1) + (pi2 + pi3);
             long long dr = 0, di = 0;
             if (!(c & 1)) {
                 const int h = c >> 1;
@@ -152,6 +170,8 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
             }
 #pragma unroll
             for (int s = 0; s < 3; ++s) {
+                if (s >= nslots)
+                    break;
                 long long inr = __shfl_up_sync(0xffffffffu, cyr[s], 1);
                 long long ini = __shfl_up_sync(0xffffffffu, cyi[s], 1);
                 const long long wrapr = __shfl_sync(0xffffffffu, s > 0 ? cyr[s - 1] : 0ll, 31);
@@ -414,7 +434,7 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
         const T magT = Mant<T>::fma_(zr, zr, zi * zi);
         mag = (float)magT;
         bool esc = magT > (T)4;
-        if (fabs((double)magT - 4.0) < 6.1035156e-5 /* 2^-14 */) {
+        if (fabs(magT - (T)4) < (T)6.1035156e-5 /* 2^-14 */) {
             // |z|^2 - 4 = D_m + 2 Re(conj(Z_m) dz) + |dz|^2, in FP64 with
             // explicit exponents (D_m exact from the orbit digits)
             const double2 zd = p.zd[m];

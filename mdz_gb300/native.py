@@ -62,6 +62,9 @@ _SIGS = {
     "mdzgpu_perturb_spacing": (C.c_int, [C.POINTER(MpValStruct), C.c_int32,
                                          C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "mdzgpu_perturb_limbs": (C.c_int32, [C.c_int64]),
+    "mdzgpu_reference_orbit": (C.c_int, [P, C.POINTER(MpValStruct), C.POINTER(MpValStruct),
+                                         C.c_int64, C.c_int32, C.c_int64, P, P, P, P,
+                                         C.POINTER(C.c_int64)]),
     "mdzgpu_mp_max_words": (C.c_int32, []),
     "mdzgpu_fx_from_mpval": (C.c_int, [C.POINTER(MpValStruct), C.c_int32, P]),
     "mdzgpu_mp_coordinates": (C.c_int, [C.POINTER(MpValStruct)] * 3

@@ -69,3 +69,40 @@ def test_perturb_config4_samples(renderer):
     want = DATA["c4_counts"]
     frac = float((got != want).mean())
     assert frac <= 0.001, f"{frac:.5f} of the 4096 samples differ"
+
+
+@pytest.mark.parametrize("cx,cy,prec,n", [("-0.75", "0.1", 128, 60),
+                                          ("0x1p-40", "1", 320, 100),
+                                          ("-1.7497856353511106873", "0.0000153218", 1088, 200)])
+def test_reference_orbit_matches_exact(renderer, cx, cy, prec, n):
+    """The GPU's multi-limb orbit against exact rational iteration (Python
+    big integers at the same digit precision, rounded to double)."""
+    import ctypes as C
+    from fractions import Fraction
+    lib = renderer.lib
+    cxv = MpVal.from_fraction(parse_number(cx), prec)
+    cyv = MpVal.from_fraction(parse_number(cy), prec)
+    L = int(lib.mdzgpu_perturb_limbs(prec))
+    F = 28 * (L - 1)
+    zr = np.zeros(n + 1)
+    zi = np.zeros(n + 1)
+    dm = np.zeros(n + 1)
+    de = np.zeros(n + 1, np.int32)
+    ln = C.c_int64()
+    a, ka = cxv.struct()
+    b, kb = cyv.struct()
+    assert lib.mdzgpu_reference_orbit(renderer.ctx, C.byref(a), C.byref(b), prec, 0, n,
+                                      zr.ctypes.data, zi.ctypes.data, dm.ctypes.data,
+                                      de.ctypes.data, C.byref(ln)) == 0
+    # exact orbit with truncation to F fractional bits (floor), as digits hold it
+    CR = int(cxv.to_fraction() * 2 ** F)
+    CI = int(cyv.to_fraction() * 2 ** F)
+    xr, xi = CR, CI
+    for k in range(1, int(ln.value)):
+        want_r, want_i = float(Fraction(xr, 2 ** F)), float(Fraction(xi, 2 ** F))
+        tol = 2.0 ** -45 * max(1.0, abs(want_r) + abs(want_i))
+        assert abs(zr[k] - want_r) <= tol and abs(zi[k] - want_i) <= tol, k
+        d = float(Fraction(xr * xr + xi * xi, 2 ** (2 * F)) - 4)
+        got_d = float(Fraction(dm[k]) * Fraction(2) ** int(de[k]))
+        assert abs(got_d - d) <= 1e-9 * max(1e-300, abs(d)) + 2.0 ** -40, k
+        xr, xi = (xr * xr - xi * xi) // 2 ** F + CR, (2 * xr * xi) // 2 ** F + CI
