@@ -54,6 +54,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--frame", default=None,
+                    help="WxH override of the frame size (same centre, pixel spacing scaled) "
+                         "for small profiling cases")
     return ap.parse_args()
 
 
@@ -316,7 +319,15 @@ def run_ours(args, view, world, rank, local, dist):
 
 def main():
     args = parse_args()
-    view = VIEWS[args.workload]
+    view = dict(VIEWS[args.workload])
+    if args.frame:
+        from fractions import Fraction
+        from mdz_gb300 import parse_number
+        from mdz_gb300.mpval import hexfloat
+        w, h = (int(x) for x in args.frame.lower().split("x"))
+        # keep the pixel spacing: a crop around the centre
+        view["size"] = hexfloat(parse_number(view["size"]) * Fraction(w, view["width"]))
+        view["width"], view["height"] = w, h
     world, rank, local, dist = dist_init(args)
     try:
         if args.impl == "reference":

@@ -750,6 +750,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         q.stop = nullptr;
         q.list = list2;
         q.list_count = counts_dev + 1;
+        q.mag = d_mag;
         if ((rc = launch_mp(ctx, q, ctx->stream))) {
             cudaEventDestroy(evo);
             return rc;

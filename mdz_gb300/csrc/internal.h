@@ -101,6 +101,7 @@ struct MpLaunch {
     // out[list[i]] with x = xs[list[i] % W], y = ys[list[i] / W]
     const unsigned* list = nullptr;
     const unsigned* list_count = nullptr;
+    float* mag = nullptr;   // |z|^2 at escape (FP32), when non-null
 };
 int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
 bool mp_words_supported(int words);

@@ -38,9 +38,18 @@ struct CShared {
     __device__ __forceinline__ uint32_t operator()(int k) const { return base[k * stride]; }
 };
 
+// Top two words of a fixed-point number as a float (value < 128 in size).
+template <int N>
+__device__ __forceinline__ float fx_top_float(const uint32_t (&x)[N])
+{
+    return (float)(int32_t)x[N - 1] * 5.9604645e-8f /* 2^-24 */
+           + (float)x[N - 2] * 1.3877788e-17f /* 2^-56 */;
+}
+
 template <int N, int FRACTAL, class CG>
 __device__ __forceinline__ uint32_t escape_mp(uint32_t (&wre)[N], uint32_t (&wim)[N],
-                                              const CG& c_re, const CG& c_im, uint32_t depth)
+                                              const CG& c_re, const CG& c_im, uint32_t depth,
+                                              float& mag)
 {
     uint32_t wre2[N], wim2[N], acc[N + 2], t[N], d[N];
     uint32_t sre = fx::abs_inplace<N>(wre);
@@ -61,8 +70,11 @@ __device__ __forceinline__ uint32_t escape_mp(uint32_t (&wre)[N], uint32_t (&wim
         if (FRACTAL == MDZ_GENERALIZED_CELTIC || (FRACTAL == MDZ_VARIANT && (wz & 1u)))
             md = (uint32_t)((int32_t)d[N - 1] >> 31);
         fx::add_signed<N>(c_re, d, md, wre);
-        if (fx::big<N>(wre) || fx::big<N>(wim))
+        if (fx::big<N>(wre) || fx::big<N>(wim)) {
+            const float a = fx_top_float<N>(wre), b = fx_top_float<N>(wim);
+            mag = a * a + b * b;
             return wz;
+        }
         sre = fx::abs_inplace<N>(wre);
         sim = fx::abs_inplace<N>(wim);
         // wim2 = wim * wim; wre2 = wre * wre
@@ -70,9 +82,12 @@ __device__ __forceinline__ uint32_t escape_mp(uint32_t (&wre)[N], uint32_t (&wim
         fx::extract<N, 24>(acc, wim2);
         fx::sqr_trunc<N>(wre, acc);
         fx::extract<N, 24>(acc, wre2);
-        if (fx::sum_gt4<N>(wim2, wre2))
+        if (fx::sum_gt4<N>(wim2, wre2)) {
+            mag = fx_top_float<N>(wim2) + fx_top_float<N>(wre2);
             return wz;
+        }
     }
+    mag = fx_top_float<N>(wim2) + fx_top_float<N>(wre2);
     return 0;
 }
 
@@ -138,6 +153,7 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
                 wim[k] = ys[k];
             }
             uint32_t n;
+            float mag = 0.f;
             if constexpr (c_in_smem<N>()) {
                 const int stride = blockDim.x;
                 uint32_t* cre = smem + threadIdx.x;
@@ -148,7 +164,7 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
                     cim[k * stride] = JULIA ? p.julia[N + k] : wim[k];
                 }
                 CShared<N> gr{cre, stride}, gi{cim, stride};
-                n = escape_mp<N, FRACTAL>(wre, wim, gr, gi, p.depth);
+                n = escape_mp<N, FRACTAL>(wre, wim, gr, gi, p.depth, mag);
             } else {
                 CRegs<N> gr, gi;
 #pragma unroll
@@ -156,9 +172,11 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
                     gr.w[k] = JULIA ? p.julia[k] : wre[k];
                     gi.w[k] = JULIA ? p.julia[N + k] : wim[k];
                 }
-                n = escape_mp<N, FRACTAL>(wre, wim, gr, gi, p.depth);
+                n = escape_mp<N, FRACTAL>(wre, wim, gr, gi, p.depth, mag);
             }
             p.out[(size_t)lrow * p.W + ix] = (int32_t)n;
+            if (p.mag)
+                p.mag[(size_t)lrow * p.W + ix] = mag;
             its = n ? n : p.depth;
         }
         its = warp_sum_u64(its);

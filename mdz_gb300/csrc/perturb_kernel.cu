@@ -311,6 +311,7 @@ struct PixState {
     T s;            // 2^e (0 below the range)
     T s2x4;         // 4 * 2^(2e), 0 when 2^(2e) underflows
     T dcr, dci;     // dc * 2^-e
+    bool careful;   // slow_if_tiny || force_slow
     bool slow_if_tiny;
     bool force_slow;
 };
@@ -326,6 +327,7 @@ __device__ __forceinline__ void refresh_scale(PixState<T>& st, T dcm_r, T dcm_i,
     // dc * 2^-e would overflow (dz far below dc); a pixel with dc == 0
     // is the reference point itself and never needs it.
     st.force_slow = (dcm_r != (T)0 || dcm_i != (T)0) && (dce - st.e) > Mant<T>::kForceSlow;
+    st.careful = st.slow_if_tiny || st.force_slow;
 }
 
 // Set t, e from a double pair scaled by 2^E.
@@ -350,6 +352,86 @@ __device__ __forceinline__ int dexp_of(double x)
     return x == 0.0 ? -100000 : ilogb(x);
 }
 
+// ---- rare paths, kept out of the hot loop's instruction stream ----
+
+// dz <- Z_m + dz, m <- 0 (Zhuoran's rebase; at the end of the orbit, or when
+// |Z_m + dz| < |dz|).  Adds the bits the sum cancelled to `lost`.  When
+// `only_if_glitch`, rebases only if |Z_m + dz| < |dz| and returns whether it
+// did.
+template <class T>
+__device__ __forceinline__ bool rebase_fp64(const PerturbLaunch& p, int m, PixState<T>& st,
+                                         T dcf_r, T dcf_i, int dce, float& lost,
+                                         bool only_if_glitch)
+{
+    const double2 zd = p.zd[m];
+    const int ze = p.ze[m];
+    const int E = max(dexp_of(fmax(fabs(zd.x), fabs(zd.y))) + ze, st.e + 40);
+    const double dr = ldexp((double)st.tr, st.e - E), di = ldexp((double)st.ti, st.e - E);
+    const double fr = ldexp(zd.x, ze - E) + dr, fi = ldexp(zd.y, ze - E) + di;
+    const double z2 = fr * fr + fi * fi, d2 = dr * dr + di * di;
+    if (only_if_glitch && !(z2 < d2))
+        return false;
+    if (d2 > z2 && z2 > 0.0)
+        lost += 0.5f * (float)log2(d2 / z2);
+    set_from_double(st, fr, fi, E);
+    refresh_scale(st, dcf_r, dcf_i, dce);
+    return true;
+}
+
+// full floatexp step in FP64: dz' = 2 Z dz + dz^2 + dc
+template <class T>
+__device__ __forceinline__ void slow_step(const PerturbLaunch& p, int m, PixState<T>& st, T dcf_r,
+                                       T dcf_i, double dcm_r, double dcm_i, int dce)
+{
+    const double2 zd = p.zd[m];
+    const int ze = p.ze[m];
+    const double tr = (double)st.tr, ti = (double)st.ti;
+    const double ar = 2.0 * (zd.x * tr - zd.y * ti), ai = 2.0 * (zd.x * ti + zd.y * tr);
+    const int ae = ze + st.e;
+    const double br = tr * tr - ti * ti, bi = 2.0 * tr * ti;
+    const int be = 2 * st.e;
+    const int E = max(max(dexp_of(fmax(fabs(ar), fabs(ai))) + ae,
+                          dexp_of(fmax(fabs(br), fabs(bi))) + be),
+                      dexp_of(fmax(fabs(dcm_r), fabs(dcm_i))) + dce);
+    const double rr = ldexp(ar, ae - E) + ldexp(br, be - E) + ldexp(dcm_r, dce - E);
+    const double ri = ldexp(ai, ae - E) + ldexp(bi, be - E) + ldexp(dcm_i, dce - E);
+    set_from_double(st, rr, ri, E);
+    refresh_scale(st, dcf_r, dcf_i, dce);
+}
+
+// |z|^2 > 4 decided from D_m = |Z_m|^2 - 4 (exact, from the orbit digits):
+// |z|^2 - 4 = D_m + 2 Re(conj(Z_m) dz) + |dz|^2, in FP64 with exponents.
+template <class T>
+__device__ __forceinline__ bool escape_exact(const PerturbLaunch& p, int m, const PixState<T>& st)
+{
+    const double2 zd = p.zd[m];
+    const int ze = p.ze[m];
+    const double dd = p.dd[m];
+    const int de = p.de[m];
+    const double t2 = 2.0 * (zd.x * (double)st.tr + zd.y * (double)st.ti);
+    const int e2 = ze + st.e;
+    const double t3 = (double)st.tr * st.tr + (double)st.ti * st.ti;
+    const int e3 = 2 * st.e;
+    const int E = max(max(dexp_of(dd) + de, dexp_of(t2) + e2), dexp_of(t3) + e3);
+    const double v = ldexp(dd, de - E) + ldexp(t2, e2 - E) + ldexp(t3, e3 - E);
+    return v > 0.0;
+}
+
+template <class T>
+__device__ __forceinline__ void load_z(const PerturbLaunch& p, int m, T& zx, T& zy)
+{
+    if (sizeof(T) == 4) {
+        const float2 z = p.zf[m];
+        zx = (T)z.x;
+        zy = (T)z.y;
+    } else {
+        const double2 zd = p.zd[m];
+        const int ze = p.ze[m];
+        zx = (T)(ze ? ldexp(zd.x, ze) : zd.x);
+        zy = (T)(ze ? ldexp(zd.y, ze) : zd.y);
+    }
+}
+
 // One pixel.  Returns the count; mag_out gets |z|^2 at escape.  `lost`
 // accumulates the bits cancelled by rebases (log2 |dz| / |z| at each one):
 // a pixel whose deltas lost more than the mantissa can spare is re-run by
@@ -364,52 +446,22 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
     refresh_scale(st, dcf_r, dcf_i, dce);
     int m = 1;
     const int K = *p.orbit_len;  // entries 0..K-1 valid
-    float2 Zf = p.zf[1];
-    T Zx = (T)Zf.x, Zy = (T)Zf.y;
-    if (sizeof(T) == 8) {
-        const double2 zd = p.zd[1];
-        if (p.ze[1] == 0) {
-            Zx = (T)zd.x;
-            Zy = (T)zd.y;
-        }
-    }
-    float mag = 0.f;
+    T Zx, Zy;
+    load_z<T>(p, 1, Zx, Zy);
+    const T band_lo = (T)4 - (T)6.1035156e-5;  // 4 - 2^-14
+    const T band_hi = (T)4 + (T)6.1035156e-5;
+    T magT = (T)0;
     for (uint32_t wz = 1; wz <= p.depth; ++wz) {
         if (m >= K - 1) {
             // end of the reference orbit: rebase onto Z_0 = 0
-            const double2 zd = p.zd[m];
-            const int ze = p.ze[m];
-            const int E = max(dexp_of(fmax(fabs(zd.x), fabs(zd.y))) + ze, st.e + 40);
-            const double dr = ldexp((double)st.tr, st.e - E), di = ldexp((double)st.ti, st.e - E);
-            const double zr = ldexp(zd.x, ze - E) + dr;
-            const double zi = ldexp(zd.y, ze - E) + di;
-            const double z2 = zr * zr + zi * zi, d2 = dr * dr + di * di;
-            if (d2 > z2 && z2 > 0.0)
-                lost += 0.5f * (float)log2(d2 / z2);
-            set_from_double(st, zr, zi, E);
-            refresh_scale(st, dcf_r, dcf_i, dce);
+            rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, lost, false);
             m = 0;
             Zx = (T)0;
             Zy = (T)0;
             ++rebases;
         }
-        const T zm2 = Zx * Zx + Zy * Zy;
-        if (st.force_slow || (st.slow_if_tiny && zm2 < (T)Mant<T>::kTinyZ2)) {
-            // full floatexp step in FP64: dz' = 2 Z dz + dz^2 + dc
-            const double2 zd = p.zd[m];
-            const int ze = p.ze[m];
-            const double tr = (double)st.tr, ti = (double)st.ti;
-            const double ar = 2.0 * (zd.x * tr - zd.y * ti), ai = 2.0 * (zd.x * ti + zd.y * tr);
-            const int ae = ze + st.e;
-            const double br = tr * tr - ti * ti, bi = 2.0 * tr * ti;
-            const int be = 2 * st.e;
-            const int E = max(max(dexp_of(fmax(fabs(ar), fabs(ai))) + ae,
-                                  dexp_of(fmax(fabs(br), fabs(bi))) + be),
-                              dexp_of(fmax(fabs(dcm_r), fabs(dcm_i))) + dce);
-            const double rr = ldexp(ar, ae - E) + ldexp(br, be - E) + ldexp(dcm_r, dce - E);
-            const double ri = ldexp(ai, ae - E) + ldexp(bi, be - E) + ldexp(dcm_i, dce - E);
-            set_from_double(st, rr, ri, E);
-            refresh_scale(st, dcf_r, dcf_i, dce);
+        if (st.careful && (st.force_slow || Zx * Zx + Zy * Zy < (T)Mant<T>::kTinyZ2)) {
+            slow_step<T>(p, m, st, dcf_r, dcf_i, dcm_r, dcm_i, dce);
         } else {
             const T tr = st.tr, ti = st.ti;
             const T u = tr + tr, v = ti + ti;
@@ -419,57 +471,23 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
             st.ti = Mant<T>::fma_(Zx, v, Mant<T>::fma_(Zy, u, Mant<T>::fma_(st.s, b, st.dci)));
         }
         ++m;
-        if (sizeof(T) == 4) {
-            Zf = p.zf[m];
-            Zx = (T)Zf.x;
-            Zy = (T)Zf.y;
-        } else {
-            const double2 zd = p.zd[m];
-            const int ze = p.ze[m];
-            Zx = (T)(ze ? ldexp(zd.x, ze) : zd.x);
-            Zy = (T)(ze ? ldexp(zd.y, ze) : zd.y);
-        }
+        load_z<T>(p, m, Zx, Zy);
         const T zr = Mant<T>::fma_(st.s, st.tr, Zx);
         const T zi = Mant<T>::fma_(st.s, st.ti, Zy);
-        const T magT = Mant<T>::fma_(zr, zr, zi * zi);
-        mag = (float)magT;
-        bool esc = magT > (T)4;
-        if (fabs(magT - (T)4) < (T)6.1035156e-5 /* 2^-14 */) {
-            // |z|^2 - 4 = D_m + 2 Re(conj(Z_m) dz) + |dz|^2, in FP64 with
-            // explicit exponents (D_m exact from the orbit digits)
-            const double2 zd = p.zd[m];
-            const int ze = p.ze[m];
-            const double dd = p.dd[m];
-            const int de = p.de[m];
-            const double t2 = 2.0 * (zd.x * (double)st.tr + zd.y * (double)st.ti);
-            const int e2 = ze + st.e;
-            const double t3 = (double)st.tr * st.tr + (double)st.ti * st.ti;
-            const int e3 = 2 * st.e;
-            const int E = max(max(dexp_of(dd) + de, dexp_of(t2) + e2), dexp_of(t3) + e3);
-            const double v = ldexp(dd, de - E) + ldexp(t2, e2 - E) + ldexp(t3, e3 - E);
-            esc = v > 0.0;
+        magT = Mant<T>::fma_(zr, zr, zi * zi);
+        if (magT > band_lo) {
+            // within 2^-14 of the bailout the rounded Z_m can not decide it
+            if (magT > band_hi || escape_exact<T>(p, m, st)) {
+                mag_out = (float)magT;
+                return wz;
+            }
         }
-        if (esc) {
-            mag_out = mag;
-            return wz;
-        }
+        // rebase test |Z_m + dz| < |dz|: it can only hold when
+        // |dz| >= |Z_m| / 2 (or |Z_m| is tiny), checked exactly in FP64
         const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
         const T zn2 = Mant<T>::fma_(Zx, Zx, Zy * Zy);
-        const bool maybe =
-            st.e >= Mant<T>::kSqExp ? (st.s2x4 * dd >= zn2) : (zn2 < (T)Mant<T>::kGlitchZ2);
-        if (maybe) {
-            // rebase test |Z_m + dz| < |dz| in FP64
-            const double2 zd = p.zd[m];
-            const int ze = p.ze[m];
-            const int E = max(dexp_of(fmax(fabs(zd.x), fabs(zd.y))) + ze, st.e + 40);
-            const double dr = ldexp((double)st.tr, st.e - E), di = ldexp((double)st.ti, st.e - E);
-            const double fr = ldexp(zd.x, ze - E) + dr, fi = ldexp(zd.y, ze - E) + di;
-            const double z2 = fr * fr + fi * fi, d2 = dr * dr + di * di;
-            if (z2 < d2) {
-                if (z2 > 0.0)
-                    lost += 0.5f * (float)log2(d2 / z2);
-                set_from_double(st, fr, fi, E);
-                refresh_scale(st, dcf_r, dcf_i, dce);
+        if (Mant<T>::fma_(st.s2x4, dd, -zn2) >= (T)0 || zn2 < (T)Mant<T>::kGlitchZ2) {
+            if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, lost, true)) {
                 m = 0;
                 Zx = (T)0;
                 Zy = (T)0;
@@ -477,17 +495,21 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
                 continue;
             }
         }
-        const T amax = fmax(fabs(st.tr), fabs(st.ti));
-        if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
-            const int k = Mant<T>::exponent_of(amax);
-            const T sc = Mant<T>::scale((T)1, -k);
-            st.tr *= sc;
-            st.ti *= sc;
-            st.e += k;
-            refresh_scale(st, dcf_r, dcf_i, dce);
+        // keep |t| in [2^-32, 2^32]; it changes by at most ~2^3 a step, so
+        // checking every 4th step is enough
+        if ((wz & 3u) == 0u) {
+            const T amax = fmax(fabs(st.tr), fabs(st.ti));
+            if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
+                const int k = Mant<T>::exponent_of(amax);
+                const T sc = Mant<T>::scale((T)1, -k);
+                st.tr *= sc;
+                st.ti *= sc;
+                st.e += k;
+                refresh_scale(st, dcf_r, dcf_i, dce);
+            }
         }
     }
-    mag_out = mag;
+    mag_out = (float)magT;
     return 0;
 }
 
