@@ -160,6 +160,34 @@ int64_t mdzo_render_fp64(int W, int H, int aa, int64_t depth, int family, int fr
     return j.pixel_iters;
 }
 
+/* Rows [row0, row0 + nrows) of a W x H frame into out (nrows x W). */
+int64_t mdzo_render_fp64_rows(int W, int H, int row0, int nrows, int64_t depth, int family,
+                              int fractal, double xmin, double xmax, double ymax, double jre,
+                              double jim, int nthreads, int32_t* out)
+{
+    frame_job j;
+    memset(&j, 0, sizeof j);
+    j.W = W;
+    j.H = row0 + nrows;
+    j.aa = 1;
+    j.next_line = row0;
+    j.depth = depth;
+    j.family = family;
+    j.fractal = fractal;
+    j.xmin = xmin;
+    j.xmax = xmax;
+    j.ymax = ymax;
+    j.jre = jre;
+    j.jim = jim;
+    j.out = out - (size_t)row0 * W;
+    j.nthreads = nthreads;
+    (void)H;
+    pthread_mutex_init(&j.mu, 0);
+    run_pool(&j, fp64_worker);
+    pthread_mutex_destroy(&j.mu);
+    return j.pixel_iters;
+}
+
 /* One Mandelbrot-family pixel through the double loop (z0 = c). */
 int64_t mdzo_point_fp64(int fractal, int64_t depth, double c_re, double c_im)
 {

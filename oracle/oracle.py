@@ -32,6 +32,9 @@ def lib() -> C.CDLL:
         L.mdzo_render_fp64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int,
                                        C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_int, C.c_void_p]
+        L.mdzo_render_fp64_rows.restype = C.c_int64
+        L.mdzo_render_fp64_rows.argtypes = [C.c_int] * 4 + [C.c_int64, C.c_int, C.c_int] + \
+            [C.c_double] * 5 + [C.c_int, C.c_void_p]
         L.mdzo_point_fp64.restype = C.c_int64
         L.mdzo_point_fp64.argtypes = [C.c_int, C.c_int64, C.c_double, C.c_double]
         L.mdzo_has_mpfr.restype = C.c_int
@@ -62,6 +65,14 @@ def render_fp64(W, H, depth, xmin, xmax, ymax, family=0, fractal=0, julia=(0.0, 
     its = lib().mdzo_render_fp64(W, H, aa, depth, family, fractal, xmin, xmax, ymax, julia[0],
                                  julia[1], threads, out.ctypes.data)
     return out, int(its)
+
+
+def render_fp64_rows(W, H, row0, nrows, depth, xmin, xmax, ymax, family=0, fractal=0,
+                     julia=(0.0, 0.0), threads=1):
+    out = np.empty((nrows, W), np.int32)
+    lib().mdzo_render_fp64_rows(W, H, row0, nrows, depth, family, fractal, xmin, xmax, ymax,
+                                julia[0], julia[1], threads, out.ctypes.data)
+    return out
 
 
 def render_mpfr(W, H, depth, prec, xmin, ymax, width, family=0, fractal=0, julia=None,
