@@ -529,8 +529,8 @@ int32_t mdzgpu_perturb_limbs(int64_t precision)
 
 // Bits a pass may lose to rebase cancellation before its pixel is re-run by
 // the next, more precise pass (FP32 -> FP64 -> multi-limb).
-constexpr float kLostLimitFp32 = 2.0f;
-constexpr float kLostLimitFp64 = 10.0f;
+constexpr float kLostLimitFp32 = 1.0f;
+constexpr float kLostLimitFp64 = 6.0f;
 
 // Fixed-point pixel coordinates of the perturbation geometry for the
 // multi-limb pass: x[ix] = cx + (2 ix - W) hs, y[line] = cy + (H - 2 line) hs.

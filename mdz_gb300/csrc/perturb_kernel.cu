@@ -73,44 +73,49 @@ __device__ void digits_to_double(const int* d, int n, int scale, double& m, int&
     }
 }
 
-// The serial part: one warp iterates Z_{k+1} = Z_k^2 + C and stores the raw
-// digits of every Z_k (re then im, L each) to HBM.  Everything else about
-// each Z_k (FP64 / FP32 roundings, |Z_k|^2 - 4) is done afterwards by
-// orbit_finish_kernel, in parallel over k, so this loop carries only the
-// multi-limb arithmetic.
-__global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
+// The serial part: Z_{k+1} = Z_k^2 + C, storing the raw digits of every Z_k
+// (re then im, L each) to HBM.  Two warps: warp 0 forms the columns of
+// Re = Zr^2 - Zi^2 + Cr, warp 1 those of Im = 2 Zr Zi + Ci, each lane one
+// column per 32-column slot; both read the packed (re, im) digit pairs from
+// shared memory with 64-bit loads.  Two shuffle passes leave every digit
+// within 2^27 + 2^5 of zero, small enough for the next product's 64-bit
+// column sums.  Everything else about each Z_k (FP64 / FP32 roundings,
+// |Z_k|^2 - 4) is done afterwards by orbit_finish_kernel, in parallel over
+// k, so this loop carries only the multi-limb arithmetic.
+__global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
 {
-    __shared__ int zr[kMaxOrbitLimbs], zi[kMaxOrbitLimbs], cr[kMaxOrbitLimbs], ci[kMaxOrbitLimbs];
-    const int lane = threadIdx.x;
+    __shared__ int2 z[kMaxOrbitLimbs];
+    __shared__ int cc[2][kMaxOrbitLimbs];
+    const int lane = threadIdx.x & 31;
+    const int part = threadIdx.x >> 5;  // 0: real, 1: imaginary
     const int L = p.limbs;
-    for (int j = lane; j < L; j += 32) {
-        cr[j] = p.c_re[j];
-        ci[j] = p.c_im[j];
-        zr[j] = p.c_re[j];
-        zi[j] = p.c_im[j];
+    for (int j = threadIdx.x; j < L; j += 64) {
+        cc[0][j] = p.c_re[j];
+        cc[1][j] = p.c_im[j];
+        z[j] = make_int2(p.c_re[j], p.c_im[j]);
         p.digits[j] = 0;                    // Z_0 = 0
         p.digits[L + j] = 0;
         p.digits[2 * L + j] = p.c_re[j];    // Z_1 = C
         p.digits[3 * L + j] = p.c_im[j];
     }
-    __syncwarp();
     const int cbase = L - 4;       // lowest column computed (3 guard columns)
     const int ctop = 2 * L - 2;    // highest column
     const int nslots = (ctop - cbase + 32) / 32;
+    const int* cpart = cc[part];
     int k = 1;
     for (;; ++k) {
-        // escape test on the two top digits (FP32 is enough to stop the
-        // orbit: stopping a step early or late only moves a rebase)
-        int escaped = 0;
-        if (lane == 0) {
-            const float a = (float)zr[L - 1] + (float)zr[L - 2] * 3.7252903e-9f;
-            const float b = (float)zi[L - 1] + (float)zi[L - 2] * 3.7252903e-9f;
-            escaped = a * a + b * b > 4.0f;
+        __syncthreads();  // Z_k complete in shared memory
+        // escape test on the two top digits, evaluated by every thread
+        // (FP32 is enough to stop the orbit: stopping a step early or late
+        // only moves a rebase)
+        {
+            const int2 t1 = z[L - 1], t2 = z[L - 2];
+            const float a = (float)t1.x + (float)t2.x * 3.7252903e-9f;
+            const float b = (float)t1.y + (float)t2.y * 3.7252903e-9f;
+            if (a * a + b * b > 4.0f || k >= p.max_k)
+                break;
         }
-        escaped = __shfl_sync(0xffffffffu, escaped, 0);
-        if (escaped || k >= p.max_k)
-            break;
-        long long vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+        long long v[3] = {0, 0, 0};
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
             const int c = cbase + lane + 32 * s;
@@ -118,87 +123,82 @@ __global__ void __launch_bounds__(32) orbit_kernel(OrbitLaunch p)
                 continue;
             const int ilo = c - (L - 1) > 0 ? c - (L - 1) : 0;
             const int ihi = (c - 1) >> 1;  // i < j = c - i
-            // four independent accumulator pairs: the pair loop is bound by
-            // shared-memory and IMAD latency, not throughput
-            long long pr0 = 0, pi0 = 0, pr1 = 0, pi1 = 0, pr2 = 0, pi2 = 0, pr3 = 0, pi3 = 0;
+            long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
             int i = ilo;
-            for (; i + 3 <= ihi; i += 4) {
-                const int j = c - i;
-                const long long a0 = zr[i], b0 = zi[i], c0 = zr[j], d0 = zi[j];
-                const long long a1 = zr[i + 1], b1 = zi[i + 1], c1 = zr[j - 1], d1 = zi[j - 1];
-                const long long a2 = zr[i + 2], b2 = zi[i + 2], c2 = zr[j - 2], d2 = zi[j - 2];
-                const long long a3 = zr[i + 3], b3 = zi[i + 3], c3 = zr[j - 3], d3 = zi[j - 3];
-                pr0 += a0 * c0 - b0 * d0;
-                pi0 += a0 * d0 + c0 * b0;
-                pr1 += a1 * c1 - b1 * d1;
-                pi1 += a1 * d1 + c1 * b1;
-                pr2 += a2 * c2 - b2 * d2;
-                pi2 += a2 * d2 + c2 * b2;
-                pr3 += a3 * c3 - b3 * d3;
-                pi3 += a3 * d3 + c3 * b3;
+            if (part == 0) {
+                for (; i + 3 <= ihi; i += 4) {
+                    const int j = c - i;
+                    const int2 p0 = z[i], q0 = z[j], p1 = z[i + 1], q1 = z[j - 1];
+                    const int2 p2 = z[i + 2], q2 = z[j - 2], p3 = z[i + 3], q3 = z[j - 3];
+                    a0 += (long long)p0.x * q0.x - (long long)p0.y * q0.y;
+                    a1 += (long long)p1.x * q1.x - (long long)p1.y * q1.y;
+                    a2 += (long long)p2.x * q2.x - (long long)p2.y * q2.y;
+                    a3 += (long long)p3.x * q3.x - (long long)p3.y * q3.y;
+                }
+                for (; i <= ihi; ++i) {
+                    const int2 pi = z[i], qj = z[c - i];
+                    a0 += (long long)pi.x * qj.x - (long long)pi.y * qj.y;
+                }
+            } else {
+                for (; i + 3 <= ihi; i += 4) {
+                    const int j = c - i;
+                    const int2 p0 = z[i], q0 = z[j], p1 = z[i + 1], q1 = z[j - 1];
+                    const int2 p2 = z[i + 2], q2 = z[j - 2], p3 = z[i + 3], q3 = z[j - 3];
+                    a0 += (long long)p0.x * q0.y + (long long)q0.x * p0.y;
+                    a1 += (long long)p1.x * q1.y + (long long)q1.x * p1.y;
+                    a2 += (long long)p2.x * q2.y + (long long)q2.x * p2.y;
+                    a3 += (long long)p3.x * q3.y + (long long)q3.x * p3.y;
+                }
+                for (; i <= ihi; ++i) {
+                    const int2 pi = z[i], qj = z[c - i];
+                    a0 += (long long)pi.x * qj.y + (long long)qj.x * pi.y;
+                }
             }
-            for (; i <= ihi; ++i) {
-                const int j = c - i;
-                const long long ari = zr[i], aii = zi[i], arj = zr[j], aij = zi[j];
-                pr0 += ari * arj - aii * aij;
-                pi0 += ari * aij + arj * aii;
-            }
-            const long long pr = (pr0 + pr1) + (pr2 + pr3), pi = (pi0 + pi1) + (pi2 + pi3);
-            long long dr = 0, di = 0;
+            long long acc = 2 * ((a0 + a1) + (a2 + a3));
             if (!(c & 1)) {
-                const int h = c >> 1;
-                const long long a = zr[h], b = zi[h];
-                dr = a * a - b * b;
-                di = a * b;
+                const int2 h = z[c >> 1];
+                acc += part == 0 ? (long long)h.x * h.x - (long long)h.y * h.y
+                                 : 2 * (long long)h.x * h.y;
             }
-            vr[s] = 2 * pr + dr;
-            vi[s] = 2 * (pi + di);
-            if (c >= L - 1) {
-                vr[s] += cr[c - (L - 1)];
-                vi[s] += ci[c - (L - 1)];
-            }
+            if (c >= L - 1)
+                acc += cpart[c - (L - 1)];
+            v[s] = acc;
         }
-        // carry propagation: three passes; column c+1 is lane+1 (slot s) or
-        // lane 0 of slot s+1
+        // carry propagation: column c+1 is lane+1 (slot s) or lane 0 of
+        // slot s+1; two passes bound every digit by 2^27 + 2^5
 #pragma unroll
-        for (int pass = 0; pass < 3; ++pass) {
-            long long dgr[3], dgi[3], cyr[3], cyi[3];
+        for (int pass = 0; pass < 2; ++pass) {
+            long long dg[3], cy[3];
 #pragma unroll
-            for (int s = 0; s < 3; ++s) {
-                digit_split(vr[s], dgr[s], cyr[s]);
-                digit_split(vi[s], dgi[s], cyi[s]);
-            }
+            for (int s = 0; s < 3; ++s)
+                digit_split(v[s], dg[s], cy[s]);
 #pragma unroll
             for (int s = 0; s < 3; ++s) {
                 if (s >= nslots)
                     break;
-                long long inr = __shfl_up_sync(0xffffffffu, cyr[s], 1);
-                long long ini = __shfl_up_sync(0xffffffffu, cyi[s], 1);
-                const long long wrapr = __shfl_sync(0xffffffffu, s > 0 ? cyr[s - 1] : 0ll, 31);
-                const long long wrapi = __shfl_sync(0xffffffffu, s > 0 ? cyi[s - 1] : 0ll, 31);
-                if (lane == 0) {
-                    inr = wrapr;
-                    ini = wrapi;
-                }
-                vr[s] = dgr[s] + inr;
-                vi[s] = dgi[s] + ini;
+                long long in = __shfl_up_sync(0xffffffffu, cy[s], 1);
+                const long long wrap = __shfl_sync(0xffffffffu, s > 0 ? cy[s - 1] : 0ll, 31);
+                if (lane == 0)
+                    in = wrap;
+                v[s] = dg[s] + in;
             }
         }
-        __syncwarp();
-        int* out = p.digits + (size_t)(k + 1) * 2 * L;
+        __syncthreads();  // every read of Z_k done
+        int* out = p.digits + (size_t)(k + 1) * 2 * L + part * L;
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
             const int c = cbase + lane + 32 * s;
-            if (c <= ctop && c >= L - 1) {
-                zr[c - (L - 1)] = (int)vr[s];
-                zi[c - (L - 1)] = (int)vi[s];
-                out[c - (L - 1)] = (int)vr[s];
-                out[L + c - (L - 1)] = (int)vi[s];
+            if (s < nslots && c <= ctop && c >= L - 1) {
+                const int d = (int)v[s];
+                if (part == 0)
+                    z[c - (L - 1)].x = d;
+                else
+                    z[c - (L - 1)].y = d;
+                out[c - (L - 1)] = d;
             }
         }
-        __syncwarp();
     }
-    if (lane == 0)
+    if (threadIdx.x == 0)
         *p.out_len = k + 1;  // entries 0..k are valid
 }
 
@@ -595,7 +595,7 @@ int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
         set_error("orbit: %d limbs outside [5, %d]", p.limbs, kMaxOrbitLimbs);
         return MDZGPU_ERR_UNSUPPORTED;
     }
-    orbit_kernel<<<1, 32, 0, s>>>(p);
+    orbit_kernel<<<1, 64, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
     orbit_finish_kernel<<<(p.max_k + 1 + 127) / 128, 128, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());

@@ -1,9 +1,10 @@
 """Perturbation method on the GPU, scored against MPFR at twice the
 precision (fixtures from the oracle's MPFR loop, tests/golden/perturb.npz).
 
-Bar: at most 0.1% of pixels differ in iteration count from the 2x-precision
-MPFR oracle; the smooth-colour error nu = n + 1 - log2(log2|z_n|^2 / 2) is
-reported and bounded for pixels whose count matches."""
+Bar: at most 0.1% of pixels (at least 2 on these small frames) differ in
+iteration count from the 2x-precision MPFR oracle; the smooth-colour error
+nu = n + 1 - log2(log2|z_n|^2 / 2) against the oracle's is reported (printed)
+and its 99th percentile over count-matching pixels bounded by 0.01."""
 import json
 import math
 from pathlib import Path
@@ -43,12 +44,16 @@ def test_perturb_frame_vs_mpfr_2x(renderer, name):
     want = DATA[name]
     diff = counts != want
     frac = float(diff.mean())
-    assert frac <= 0.001 or int(diff.sum()) <= 2, f"{name}: {int(diff.sum())} pixels differ"
     ok = (~diff) & (want > 0)
+    err = np.zeros(1)
     if ok.any():
         err = np.abs(smooth(counts[ok], mag[ok].astype(np.float64))
                      - smooth(want[ok], DATA[name + "__mag"][ok]))
-        assert float(np.nanmax(err)) < 0.05, f"smooth-colour error {np.nanmax(err)}"
+    print(f"{name}: count error {int(diff.sum())}/{diff.size} pixels; smooth-colour error "
+          f"p99 {np.nanpercentile(err, 99):.2e} max {np.nanmax(err):.2e}; escalated "
+          f"fp64 {st['escalated_fp64']} mp {st['escalated_mp']}")
+    assert frac <= 0.001 or int(diff.sum()) <= 2, f"{name}: {int(diff.sum())} pixels differ"
+    assert float(np.nanpercentile(err, 99)) < 0.01
     assert st["pixel_iters"] > 0
 
 
@@ -68,6 +73,11 @@ def test_perturb_config4_samples(renderer):
     got = counts[ln, ix].astype(np.int64)
     want = DATA["c4_counts"]
     frac = float((got != want).mean())
+    ok = (got == want) & (want > 0)
+    err = np.abs(smooth(got[ok], mag[ln, ix][ok].astype(np.float64))
+                 - smooth(want[ok], DATA["c4_mag"][ok])) if ok.any() else np.zeros(1)
+    print(f"config 4: {int((got != want).sum())}/4096 samples differ; smooth-colour error "
+          f"max {np.nanmax(err):.2e}")
     assert frac <= 0.001, f"{frac:.5f} of the 4096 samples differ"
 
 
