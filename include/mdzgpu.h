@@ -169,6 +169,26 @@ int mdzgpu_render_mp_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
                             const mdzgpu_mpval* julia_im, int64_t precision,
                             int32_t words, int32_t* d_counts,
                             mdzgpu_stats* st);
+/* No counterpart in the reference.  mdzgpu_render_mp without any device
+ * allocation, for callers that may not allocate GPU memory (a plugin whose
+ * host application's pool allocator owns the device, or a render loop that
+ * cannot take cudaMalloc's implicit device synchronisation).  Same inputs and
+ * results as mdzgpu_render_mp_device; d_counts is the caller's device buffer
+ * of width*height int32; the work is queued on `stream` (a cudaStream_t,
+ * NULL = default stream) and not waited for.  Scratch is a fixed 1.13 MiB
+ * array per GPU inside the library, held until the process exits: frames
+ * with width + height > 8192 or needing more than 36 words are rejected
+ * (MDZGPU_ERR_ARG).  Calls on one stream are ordered; calls that may overlap
+ * on the GPU (other streams or threads) race on the shared scratch and must
+ * not be made.  The first call on each device looks up the scratch address
+ * (with that device current); make it before capturing a stream. */
+int mdzgpu_render_mp_noalloc(const mdzgpu_frame* f, const mdzgpu_mpval* xmin,
+                             const mdzgpu_mpval* ymax,
+                             const mdzgpu_mpval* width,
+                             const mdzgpu_mpval* julia_re,
+                             const mdzgpu_mpval* julia_im, int64_t precision,
+                             int32_t words, int32_t* d_counts, void* stream);
+
 /* Largest `words` value the MP kernel is built for. */
 int32_t mdzgpu_mp_max_words(void);
 

@@ -67,6 +67,8 @@ _SIGS = {
                                          C.POINTER(C.c_int64)]),
     "mdzgpu_mp_max_words": (C.c_int32, []),
     "mdzgpu_fx_from_mpval": (C.c_int, [C.POINTER(MpValStruct), C.c_int32, P]),
+    "mdzgpu_render_mp_noalloc": (C.c_int, [C.POINTER(Frame)] + [C.POINTER(MpValStruct)] * 5
+                                 + [C.c_int64, C.c_int32, P, P]),
     "mdzgpu_mp_coordinates": (C.c_int, [C.POINTER(MpValStruct)] * 3
                               + [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int32, P, P]),
     "mdzgpu_abi_layout": (C.c_int, [P, C.c_int]),
