@@ -285,7 +285,9 @@ def run_ours(args, view, world, rank, local, dist):
         r.close()
         return
     ms_per_step = total_ms_max / args.steps
-    pert_ms = [k - o for k, o in zip(kernel_ms, orbit_ms)]
+    # fused launches report orbit_ms = -1: the orbit runs inside the pixel
+    # kernel, so the whole kernel time is charged to the pixels
+    pert_ms = [k - (o if o > 0 else 0.0) for k, o in zip(kernel_ms, orbit_ms)]
     avg_pert_ms = sum(pert_ms) / len(pert_ms)
     achieved = (its / args.steps) * ALGO_OPS_PER_PIXEL_ITER / (avg_pert_ms * 1e-3) / 1e9
     line = {
@@ -299,7 +301,7 @@ def run_ours(args, view, world, rank, local, dist):
                    "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches * args.steps,
-        "orbit_ms": sum(orbit_ms) / len(orbit_ms),
+        "orbit_ms": (sum(orbit_ms) / len(orbit_ms)) if min(orbit_ms) >= 0 else "fused",
         "rebases_per_step": rebases / args.steps,
         "e2e": {"value": e2e_its_all / (e2e_max * 1e-3), "unit": "pixel-iters/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -653,10 +653,17 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     int64_t h2d_extra = 0;
     cudaEvent_t evo;
     MDZ_CUDA_TRY(cudaEventCreate(&evo));
+    // progress words of the fused launch live beside out_len
+    int* prog = (int*)(ob + off_len);
+    MDZ_CUDA_TRY(cudaMemsetAsync(prog, 0, 256, ctx->stream));
+    const char* fenv = getenv("MDZGPU_FUSED");
+    const bool fused = !(fenv && fenv[0] == '0');
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
-    if ((rc = launch_orbit(o, ctx->stream))) {
-        cudaEventDestroy(evo);
-        return rc;
+    if (!fused) {
+        if ((rc = launch_orbit(o, ctx->stream))) {
+            cudaEventDestroy(evo);
+            return rc;
+        }
     }
     MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->stream));
     PerturbLaunch p;
@@ -687,11 +694,17 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     unsigned* list1 = (unsigned*)((char*)ctx->lists.ptr + 256);
     unsigned* list2 = list1 + n;
     MDZ_CUDA_TRY(cudaMemsetAsync(ctx->lists.ptr, 0, 256, ctx->stream));
-    // pass 0: FP32 mantissas over the frame
+    // pass 0: FP32 mantissas over the frame (fused with the orbit unless
+    // MDZGPU_FUSED=0)
     p.lost_limit = kLostLimitFp32;
     p.flag_out = list1;
     p.flag_out_count = counts_dev;
-    if ((rc = launch_perturb(ctx, p, ctx->stream, 0))) {
+    p.raw_len = prog + 1;
+    p.fin_len = prog + 2;
+    p.orbit_done = prog + 3;
+    p.orbit_error = prog + 4;
+    rc = fused ? launch_fused(ctx, o, p, ctx->stream) : launch_perturb(ctx, p, ctx->stream, 0);
+    if (rc) {
         cudaEventDestroy(evo);
         return rc;
     }
@@ -769,17 +782,24 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     }
     unsigned long long reb = 0;
     int olen = 0;
+    int orbit_err = 0;
     unsigned esc[2] = {0, 0};
+    MDZ_CUDA_TRY(cudaMemcpyAsync(&orbit_err, prog + 4, 4, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(esc, counts_dev, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(&reb, p.rebases, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(&olen, o.out_len, 4, cudaMemcpyDeviceToHost, ctx->stream));
     rc = finish_stats(ctx, st, t0, 5, (int64_t)dig.size() * 4 + h2d_extra, d2h + 20);
+    if (!rc && orbit_err) {
+        set_error("perturbation: a bounded wait on the reference orbit gave up");
+        rc = MDZGPU_ERR_TIMEOUT;
+    }
     if (!rc && st) {
         st->escalated_fp64 = esc[0];
         st->escalated_mp = esc[1];
         float oms = 0.f;
         cudaEventElapsedTime(&oms, ctx->ev0, evo);
-        st->orbit_ms = oms;
+        // fused: the orbit runs inside the pixel kernel and has no own time
+        st->orbit_ms = fused ? -1.0 : oms;
         st->rebases = (int64_t)reb;
         st->orbit_len = olen;
     }

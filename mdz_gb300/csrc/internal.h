@@ -150,9 +150,16 @@ struct PerturbLaunch {
     unsigned* flag_out_count = nullptr;
     const unsigned* list_in = nullptr;        // list pass: pixels to render
     const unsigned* list_in_count = nullptr;
+    // fused launch: orbit progress words (device)
+    int* raw_len = nullptr;
+    int* fin_len = nullptr;
+    int* orbit_done = nullptr;
+    int* orbit_error = nullptr;
 };
 // pass 0: FP32 frame pass; pass 1: FP64 pass over list_in
 int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass);
+// Orbit + FP32 pixel pass in one cooperative launch (progress words in p).
+int launch_fused(mdzgpu_ctx* ctx, const OrbitLaunch& o, const PerturbLaunch& p, cudaStream_t s);
 
 // Fixed-point conversion helpers (host).  A fixed-point number has `words`
 // 32-bit words, two's complement, least significant first, and

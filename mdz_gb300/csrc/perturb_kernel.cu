@@ -37,6 +37,9 @@ namespace {
 constexpr int kTileW = 8;
 constexpr int kTileH = 4;
 constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
+// Bounded waits of the fused launch: ~2^25 polls of >= 256 ns (several
+// seconds), far beyond any legitimate wait, then the error flag is raised.
+constexpr int kSpinLimit = 1 << 25;
 
 // --------------------------------------------------------------------------
 // Reference orbit
@@ -82,10 +85,21 @@ __device__ void digits_to_double(const int* d, int n, int scale, double& m, int&
 // column sums.  Everything else about each Z_k (FP64 / FP32 roundings,
 // |Z_k|^2 - 4) is done afterwards by orbit_finish_kernel, in parallel over
 // k, so this loop carries only the multi-limb arithmetic.
-__global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
+// Progress words shared by the blocks of the fused launch.
+struct OrbitProgress {
+    int* raw_len;   // digit entries 0..raw_len-1 written (producer)
+    int* fin_len;   // entries 0..fin_len-1 finished (finisher)
+    int* done;      // producer stopped; final length in *out_len
+    int* error;     // a bounded wait gave up
+};
+
+// The producer, run by 64 threads (threadIdx.x < 64) with named barrier 1;
+// publishes raw_len every 32 steps when `prog` is given.
+__device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProgress* prog)
 {
     __shared__ int2 z[kMaxOrbitLimbs];
     __shared__ int cc[2][kMaxOrbitLimbs];
+    auto bar = [] { asm volatile("bar.sync 1, 64;" ::: "memory"); };
     const int lane = threadIdx.x & 31;
     const int part = threadIdx.x >> 5;  // 0: real, 1: imaginary
     const int L = p.limbs;
@@ -104,7 +118,13 @@ __global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
     const int* cpart = cc[part];
     int k = 1;
     for (;; ++k) {
-        __syncthreads();  // Z_k complete in shared memory
+        if (prog && (k & 31) == 0) {
+            __threadfence();  // this thread's digits of Z_0..Z_k
+            bar();
+            if (threadIdx.x == 0)
+                *(volatile int*)prog->raw_len = k + 1;
+        }
+        bar();  // Z_k complete in shared memory
         // escape test on the two top digits, evaluated by every thread
         // (FP32 is enough to stop the orbit: stopping a step early or late
         // only moves a rebase)
@@ -183,7 +203,7 @@ __global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
                 v[s] = dg[s] + in;
             }
         }
-        __syncthreads();  // every read of Z_k done
+        bar();  // every read of Z_k done
         int* out = p.digits + (size_t)(k + 1) * 2 * L + part * L;
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
@@ -198,8 +218,21 @@ __global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
             }
         }
     }
-    if (threadIdx.x == 0)
+    __threadfence();
+    bar();
+    if (threadIdx.x == 0) {
         *p.out_len = k + 1;  // entries 0..k are valid
+        if (prog) {
+            *(volatile int*)prog->raw_len = k + 1;
+            __threadfence();
+            *(volatile int*)prog->done = 1;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
+{
+    orbit_produce(p, nullptr);
 }
 
 // Per entry k (one thread each): the FP64 pair with its exponent, the FP32
@@ -208,15 +241,17 @@ __global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
 // because the escape test of a pixel with a tiny dz needs the sign of
 // D_k + 2 Re(conj(Z_k) dz) + |dz|^2 and FP32 / FP64 roundings of Z_k can
 // not give it when |Z_k| is within 2^-20 of 2.
-__global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
+__device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from_l2)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int len = *p.out_len;
-    if (k >= len)
-        return;
     const int L = p.limbs;
-    const int* dr = p.digits + (size_t)k * 2 * L;
-    const int* di = dr + L;
+    int dr[kMaxOrbitLimbs], di[kMaxOrbitLimbs];
+    const int* src = p.digits + (size_t)k * 2 * L;
+    for (int j = 0; j < L; ++j) {
+        // in the fused launch the digits were written by another block while
+        // this one runs: read them from L2, never from a stale L1 line
+        dr[j] = from_l2 ? __ldcg(src + j) : src[j];
+        di[j] = from_l2 ? __ldcg(src + L + j) : src[L + j];
+    }
     const int F = 28 * (L - 1);
     double mr, mi;
     int xr, xi;
@@ -269,6 +304,61 @@ __global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
     digits_to_double(dig, ncol, -2 * F, m, x);
     p.dd[k] = m;
     p.de[k] = x;
+}
+
+__global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < *p.out_len)
+        finish_entry(p, k, false);
+}
+
+// The finisher of the fused launch (one block of 256 threads): finishes the
+// orbit in batches of 256 entries as the producer publishes them and
+// publishes fin_len in whole batches, so a consumer never reads a cache line
+// holding an unfinished entry.
+__device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
+{
+    __shared__ int s_avail, s_done, s_err;
+    int fin = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int spins = 0, r = 0, d = 0, err = 0;
+            for (;;) {
+                d = *(volatile int*)g.done;
+                r = d ? *(volatile int*)p.out_len : *(volatile int*)g.raw_len;
+                if (d || r >= fin + 256)
+                    break;
+                if (*(volatile int*)g.error || ++spins > kSpinLimit) {
+                    err = 1;
+                    break;
+                }
+                __nanosleep(256);
+            }
+            s_avail = r;
+            s_done = d;
+            s_err = err;
+        }
+        __syncthreads();
+        const int avail = s_avail, dn = s_done;
+        if (s_err) {
+            if (threadIdx.x == 0)
+                atomicExch(g.error, 1);
+            return;
+        }
+        const int end = min(avail, fin + 256);
+        const int k = fin + (int)threadIdx.x;
+        if (k < end)
+            finish_entry(p, k, true);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0)
+            *(volatile int*)g.fin_len = end;
+        fin = end;
+        if (dn && fin >= avail)
+            return;
+        __syncthreads();
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -436,7 +526,39 @@ __device__ __forceinline__ void load_z(const PerturbLaunch& p, int m, T& zx, T& 
 // accumulates the bits cancelled by rebases (log2 |dz| / |z| at each one):
 // a pixel whose deltas lost more than the mantissa can spare is re-run by
 // the next, more precise, pass.
-template <class T>
+// In the fused launch (STREAM) the orbit is still being produced: entries
+// below `avail` are finished; a pixel that needs entry m + 1 waits (bounded)
+// for the finisher, and learns the final length K once the producer is done.
+// Returns false when a wait gave up (error flag raised).
+__device__ __forceinline__ bool wait_orbit(const PerturbLaunch& p, int need, int& avail, int& K)
+{
+    int spins = 0;
+    for (;;) {
+        const int f = *(volatile const int*)p.fin_len;
+        const int d = *(volatile const int*)p.orbit_done;
+        if (d) {
+            const int len = *(volatile const int*)p.orbit_len;
+            if (f >= len) {
+                avail = f;
+                K = len;
+                __threadfence();
+                return true;
+            }
+        }
+        if (f > need) {
+            avail = f;
+            __threadfence();  // acquire: the entries below f are visible
+            return true;
+        }
+        if (*(volatile const int*)p.orbit_error || ++spins > kSpinLimit) {
+            atomicExch(p.orbit_error, 1);
+            return false;
+        }
+        __nanosleep(128);
+    }
+}
+
+template <class T, bool STREAM>
 __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
                                   float& mag_out, unsigned& rebases, float& lost)
 {
@@ -445,20 +567,32 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
     set_from_double(st, dcm_r, dcm_i, dce);
     refresh_scale(st, dcf_r, dcf_i, dce);
     int m = 1;
-    const int K = *p.orbit_len;  // entries 0..K-1 valid
+    // entries 0..avail-1 readable; K = orbit length (unknown while streaming)
+    int K = STREAM ? 0x7fffffff : *p.orbit_len;
+    int avail = K;
+    if (STREAM && !wait_orbit(p, 1, avail, K)) {
+        mag_out = 0.f;
+        return 0;
+    }
     T Zx, Zy;
     load_z<T>(p, 1, Zx, Zy);
     const T band_lo = (T)4 - (T)6.1035156e-5;  // 4 - 2^-14
     const T band_hi = (T)4 + (T)6.1035156e-5;
     T magT = (T)0;
     for (uint32_t wz = 1; wz <= p.depth; ++wz) {
-        if (m >= K - 1) {
-            // end of the reference orbit: rebase onto Z_0 = 0
-            rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, lost, false);
-            m = 0;
-            Zx = (T)0;
-            Zy = (T)0;
-            ++rebases;
+        if (m + 1 >= avail) {
+            if (STREAM && m + 1 < K && !wait_orbit(p, m + 1, avail, K)) {
+                mag_out = 0.f;
+                return 0;
+            }
+            if (m >= K - 1) {
+                // end of the reference orbit: rebase onto Z_0 = 0
+                rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, lost, false);
+                m = 0;
+                Zx = (T)0;
+                Zy = (T)0;
+                ++rebases;
+            }
         }
         if (st.careful && (st.force_slow || Zx * Zx + Zy * Zy < (T)Mant<T>::kTinyZ2)) {
             slow_step<T>(p, m, st, dcf_r, dcf_i, dcm_r, dcm_i, dce);
@@ -525,8 +659,8 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 // (FP64) walks the list of pixels the previous pass flagged, in warp-sized
 // chunks.  Each pass appends the pixels it could not finish precisely to
 // p.flag_out; pixel-iterations are counted only for pixels it finalises.
-template <class T, bool WANT_MAG, bool LIST>
-__global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
+template <class T, bool WANT_MAG, bool LIST, bool STREAM>
+__device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
 {
     const int lane = threadIdx.x & 31;
     const int tiles_x = (p.W + kTileW - 1) / kTileW;
@@ -564,7 +698,7 @@ __global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
             const double dcm_r = (double)(2 * ix - p.W) * p.hs_m;
             const double dcm_i = (double)(p.H - 2 * line) * p.hs_m;
             float mag = 0.f, lost = 0.f;
-            const uint32_t n = perturb_pixel<T>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost);
+            const uint32_t n = perturb_pixel<T, STREAM>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost);
             const size_t o = (size_t)lrow * p.W + ix;
             p.out[o] = (int32_t)n;
             if (WANT_MAG)
@@ -585,6 +719,35 @@ __global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
                 atomicAdd(p.rebases, rb);
         }
     }
+}
+
+template <class T, bool WANT_MAG, bool LIST>
+__global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
+{
+    pixel_tiles<T, WANT_MAG, LIST, false>(p);
+}
+
+// One cooperative launch: block 0 produces the reference orbit (64
+// threads), block 1 finishes its entries, every other block iterates pixels
+// (FP32 pass) as soon as the entries they need are finished.  Pixel work per
+// orbit step is larger than the producer's, so the orbit's serial time hides
+// behind the pixels.  Cooperative launch guarantees the blocks are
+// co-resident; every wait is bounded and raises orbit_error on timeout.
+template <bool WANT_MAG>
+__global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, PerturbLaunch p)
+{
+    if (blockIdx.x == 0) {
+        OrbitProgress g{p.raw_len, p.fin_len, p.orbit_done, p.orbit_error};
+        if (threadIdx.x < 64)
+            orbit_produce(o, &g);
+        return;
+    }
+    if (blockIdx.x == 1) {
+        OrbitProgress g{p.raw_len, p.fin_len, p.orbit_done, p.orbit_error};
+        orbit_finisher(o, g);
+        return;
+    }
+    pixel_tiles<float, WANT_MAG, false, true>(p);
 }
 
 }  // namespace
@@ -635,6 +798,46 @@ int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int 
     const long chunks = ((long)p.W * p.nrows + 31) / 32;
     return mag ? launch_pass<double, true, true>(ctx, p, s, chunks)
                : launch_pass<double, false, true>(ctx, p, s, chunks);
+}
+
+int launch_fused(mdzgpu_ctx* ctx, const OrbitLaunch& o, const PerturbLaunch& p, cudaStream_t s)
+{
+    if (o.limbs < 5 || o.limbs > kMaxOrbitLimbs) {
+        set_error("orbit: %d limbs outside [5, %d]", o.limbs, kMaxOrbitLimbs);
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    const bool mag = p.mag != nullptr;
+    const void* fn = mag ? (const void*)perturb_fused_kernel<true>
+                         : (const void*)perturb_fused_kernel<false>;
+    static int bps[2] = {0, 0};
+    int& b = bps[mag ? 1 : 0];
+    if (!b) {
+        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, 0));
+        if (b < 1)
+            b = 1;
+    }
+    int coop = 0;
+    MDZ_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+    if (!coop) {
+        set_error("device lacks cooperative launch");
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    const long tiles = (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
+    long grid = (long)ctx->num_sms * b;          // all co-resident
+    const long needed = 2 + (tiles + 7) / 8;
+    if (grid > needed)
+        grid = needed;
+    if (grid < 3)
+        grid = 3;
+    if (grid > (long)ctx->num_sms * b) {
+        set_error("fused launch needs %ld co-resident blocks", grid);
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    OrbitLaunch oo = o;
+    PerturbLaunch pp = p;
+    void* args[] = {&oo, &pp};
+    MDZ_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(256), args, 0, s));
+    return MDZGPU_OK;
 }
 
 int orbit_max_limbs()
