@@ -656,8 +656,12 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     // progress words of the fused launch live beside out_len
     int* prog = (int*)(ob + off_len);
     MDZ_CUDA_TRY(cudaMemsetAsync(prog, 0, 256, ctx->stream));
+    // MDZGPU_FUSED=1: orbit and FP32 pixel pass in one cooperative launch.
+    // Off by default: a persistent grid holds a fraction of the frame's tiles,
+    // so the first wave is paced by the serial orbit (measured slower than
+    // the separate launches); the serving engine overlaps orbits instead.
     const char* fenv = getenv("MDZGPU_FUSED");
-    const bool fused = !(fenv && fenv[0] == '0');
+    const bool fused = fenv && fenv[0] == '1';
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
     if (!fused) {
         if ((rc = launch_orbit(o, ctx->stream))) {
@@ -694,8 +698,8 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     unsigned* list1 = (unsigned*)((char*)ctx->lists.ptr + 256);
     unsigned* list2 = list1 + n;
     MDZ_CUDA_TRY(cudaMemsetAsync(ctx->lists.ptr, 0, 256, ctx->stream));
-    // pass 0: FP32 mantissas over the frame (fused with the orbit unless
-    // MDZGPU_FUSED=0)
+    // pass 0: FP32 mantissas over the frame (fused with the orbit when
+    // MDZGPU_FUSED=1)
     p.lost_limit = kLostLimitFp32;
     p.flag_out = list1;
     p.flag_out_count = counts_dev;
@@ -703,6 +707,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.fin_len = prog + 2;
     p.orbit_done = prog + 3;
     p.orbit_error = prog + 4;
+    p.producer_sm = prog + 5;
     rc = fused ? launch_fused(ctx, o, p, ctx->stream) : launch_perturb(ctx, p, ctx->stream, 0);
     if (rc) {
         cudaEventDestroy(evo);

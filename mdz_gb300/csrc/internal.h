@@ -155,6 +155,7 @@ struct PerturbLaunch {
     int* fin_len = nullptr;
     int* orbit_done = nullptr;
     int* orbit_error = nullptr;
+    int* producer_sm = nullptr;  // SM id + 1 of the orbit producer block
 };
 // pass 0: FP32 frame pass; pass 1: FP64 pass over list_in
 int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass);

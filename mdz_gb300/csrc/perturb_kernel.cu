@@ -530,37 +530,57 @@ __device__ __forceinline__ void load_z(const PerturbLaunch& p, int m, T& zx, T& 
 // below `avail` are finished; a pixel that needs entry m + 1 waits (bounded)
 // for the finisher, and learns the final length K once the producer is done.
 // Returns false when a wait gave up (error flag raised).
-__device__ __forceinline__ bool wait_orbit(const PerturbLaunch& p, int need, int& avail, int& K)
+// Per-block copy of the orbit progress: pixel threads read shared memory;
+// one elected thread at a time refreshes it from global memory, so the
+// hundreds of thousands of waiting threads do not hammer one L2 line (which
+// would also slow the producer's fences).
+struct BlockOrbitView {
+    int fin;    // finished entries (>= 2 once valid)
+    int len;    // final length, 0 while the producer runs
+    int busy;   // a thread is refreshing
+};
+
+__device__ __forceinline__ bool wait_orbit(const PerturbLaunch& p, BlockOrbitView* v, int need,
+                                           int& avail, int& K)
 {
     int spins = 0;
     for (;;) {
-        const int f = *(volatile const int*)p.fin_len;
-        const int d = *(volatile const int*)p.orbit_done;
-        if (d) {
-            const int len = *(volatile const int*)p.orbit_len;
-            if (f >= len) {
-                avail = f;
-                K = len;
-                __threadfence();
-                return true;
-            }
+        const int f = *(volatile int*)&v->fin;
+        const int len = *(volatile int*)&v->len;
+        if (len && f >= len) {
+            avail = f;
+            K = len;
+            __threadfence();
+            return true;
         }
         if (f > need) {
             avail = f;
             __threadfence();  // acquire: the entries below f are visible
             return true;
         }
+        if (atomicCAS(&v->busy, 0, 1) == 0) {
+            const int gf = *(volatile const int*)p.fin_len;
+            const int gd = *(volatile const int*)p.orbit_done;
+            const int gl = gd ? *(volatile const int*)p.orbit_len : 0;
+            if (gf > *(volatile int*)&v->fin)
+                *(volatile int*)&v->fin = gf;
+            if (gl)
+                *(volatile int*)&v->len = gl;
+            __threadfence_block();
+            atomicExch(&v->busy, 0);
+        }
         if (*(volatile const int*)p.orbit_error || ++spins > kSpinLimit) {
             atomicExch(p.orbit_error, 1);
             return false;
         }
-        __nanosleep(128);
+        __nanosleep(256);
     }
 }
 
 template <class T, bool STREAM>
 __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
-                                  float& mag_out, unsigned& rebases, float& lost)
+                                  float& mag_out, unsigned& rebases, float& lost,
+                                  BlockOrbitView* view)
 {
     const T dcf_r = (T)dcm_r, dcf_i = (T)dcm_i;
     PixState<T> st;
@@ -570,7 +590,7 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
     // entries 0..avail-1 readable; K = orbit length (unknown while streaming)
     int K = STREAM ? 0x7fffffff : *p.orbit_len;
     int avail = K;
-    if (STREAM && !wait_orbit(p, 1, avail, K)) {
+    if (STREAM && !wait_orbit(p, view, 1, avail, K)) {
         mag_out = 0.f;
         return 0;
     }
@@ -581,7 +601,7 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
     T magT = (T)0;
     for (uint32_t wz = 1; wz <= p.depth; ++wz) {
         if (m + 1 >= avail) {
-            if (STREAM && m + 1 < K && !wait_orbit(p, m + 1, avail, K)) {
+            if (STREAM && m + 1 < K && !wait_orbit(p, view, m + 1, avail, K)) {
                 mag_out = 0.f;
                 return 0;
             }
@@ -662,6 +682,15 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 template <class T, bool WANT_MAG, bool LIST, bool STREAM>
 __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
 {
+    __shared__ BlockOrbitView view;
+    if (STREAM) {
+        if (threadIdx.x == 0) {
+            view.fin = 0;
+            view.len = 0;
+            view.busy = 0;
+        }
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const int tiles_x = (p.W + kTileW - 1) / kTileW;
     const int tiles_y = (p.nrows + kTileH - 1) / kTileH;
@@ -698,7 +727,7 @@ __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
             const double dcm_r = (double)(2 * ix - p.W) * p.hs_m;
             const double dcm_i = (double)(p.H - 2 * line) * p.hs_m;
             float mag = 0.f, lost = 0.f;
-            const uint32_t n = perturb_pixel<T, STREAM>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost);
+            const uint32_t n = perturb_pixel<T, STREAM>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost, &view);
             const size_t o = (size_t)lrow * p.W + ix;
             p.out[o] = (int32_t)n;
             if (WANT_MAG)
@@ -736,7 +765,11 @@ __global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
 template <bool WANT_MAG>
 __global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, PerturbLaunch p)
 {
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
     if (blockIdx.x == 0) {
+        if (threadIdx.x == 0)
+            *(volatile int*)p.producer_sm = (int)smid + 1;
         OrbitProgress g{p.raw_len, p.fin_len, p.orbit_done, p.orbit_error};
         if (threadIdx.x < 64)
             orbit_produce(o, &g);
@@ -747,6 +780,18 @@ __global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, Pe
         orbit_finisher(o, g);
         return;
     }
+    // The producer's latency-bound warps need their SM's issue slots: pixel
+    // blocks placed on that SM leave at once (1/152 of the pixel capacity).
+    __shared__ int s_leave;
+    if (threadIdx.x == 0) {
+        int sm = 0, spins = 0;
+        while ((sm = *(volatile const int*)p.producer_sm) == 0 && ++spins < kSpinLimit)
+            __nanosleep(64);
+        s_leave = (sm == (int)smid + 1);
+    }
+    __syncthreads();
+    if (s_leave)
+        return;
     pixel_tiles<float, WANT_MAG, false, true>(p);
 }
 
