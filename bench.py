@@ -15,7 +15,10 @@ Lines printed (rank 0, one JSON line):
             "perturbation vs plain MP on GPU" half of the metric);
   roofline  the perturbation kernel against the measured FP32 pipe peak;
   cpu_baseline  the oracle's MPFR loop (the reference's deep-zoom path at
-            1088 bits) on a bounded pixel sample, all host threads.
+            1088 bits) on a bounded pixel sample, all host threads;
+  serving   the seeded mixed request stream (mdz_gb300.stream) through the
+            serving engine: capacity (closed loop) and p50/p99 latency under
+            Poisson arrivals at 80% of that capacity (rank 0).
 --impl reference times that CPU path alone on the same metric.
 
 Multi-GPU: pixels are independent; every rank renders its own frame (weak
@@ -54,6 +57,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=32,
+                    help="requests of the seeded mixed stream for the serving latency run "
+                         "(0 = skip)")
+    ap.add_argument("--serve-seed", type=int, default=5005)
+    ap.add_argument("--serve-load", type=float, default=0.8)
     ap.add_argument("--frame", default=None,
                     help="WxH override of the frame size (same centre, pixel spacing scaled) "
                          "for small profiling cases")
@@ -208,6 +216,62 @@ def run_reference(args, view, world, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args, local) -> dict:
+    """The mixed request stream through the serving engine: first closed
+    loop (all requests submitted at once) to measure the capacity, then
+    Poisson arrivals at `serve_load` of that capacity for p50/p99 latency.
+    The second run's results must equal the first's (each request the same
+    alone or in any mix)."""
+    from mdz_gb300.serve import Server
+    from mdz_gb300.stream import load_pool, make_stream
+    pool = load_pool()
+    items = make_stream(args.serve_requests, pool, seed=args.serve_seed)
+
+    def run(arrivals):
+        reqs = [it.request(pool) for it in items]
+        with Server(local, arena_bytes=48 << 30, staging_bytes=2 << 30,
+                    queue_pixels=1 << 25) as srv:
+            t0 = time.perf_counter()
+            ids = []
+            for a, rq in zip(arrivals, reqs):
+                dt = t0 + a - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                ids.append(srv.submit(rq))
+            sts = [srv.wait(i, 900_000) for i in ids]
+            wall = time.perf_counter() - t0
+            stats = srv.stats()
+        return reqs, sts, wall, stats
+
+    reqs1, sts1, wall1, stats1 = run([0.0] * len(items))
+    its = sum(s["pixel_iters"] for s in sts1)
+    rate = args.serve_load * len(items) / wall1
+    gaps = np.array([it.gap for it in items]) / rate
+    arrivals = np.cumsum(gaps) - gaps[0]
+    reqs2, sts2, wall2, stats2 = run(list(arrivals))
+    same = all(np.array_equal(a.counts, b.counts) for a, b in zip(reqs1, reqs2))
+    lat = np.array([s["latency_ms"] for s in sts2])
+    ok = all(s["state"] == "done" for s in sts1 + sts2)
+    methods = {"perturbation": sum(1 for s in sts2 if s["method"] == 1),
+               "multi_limb": sum(1 for s in sts2 if s["method"] == 2)}
+    return {
+        "requests": len(items), "seed": args.serve_seed, "all_done": ok,
+        "stream": "sizes {240x180..1920x1080}, log2 span U[-1000,-10], prec ceil(-log2 span)+64, "
+                  "mandelbrot/burning ship/celtic 0.7/0.2/0.1, maxiter log-U[1e3,1e5]",
+        "capacity_run_s": wall1,
+        "throughput": {"value": its / wall1, "unit": "pixel-iters/s",
+                       "note": "closed loop, all requests submitted at once, through the "
+                               "public submit/wait API with host result buffers"},
+        "poisson_rate_per_s": rate, "load": args.serve_load, "poisson_run_s": wall2,
+        "latency_ms": {"p50": float(np.percentile(lat, 50, method="inverted_cdf")),
+                       "p99": float(np.percentile(lat, 99, method="inverted_cdf")),
+                       "max": float(lat.max()), "mean": float(lat.mean())},
+        "results_equal_across_runs": same,
+        "steps": stats2["steps"], "gpu_launches": stats2["launches"],
+        "device_bytes_peak": stats2["device_bytes_peak"], "methods": methods,
+    }
+
+
 def run_ours(args, view, world, rank, local, dist):
     import torch
     from mdz_gb300 import Renderer, native
@@ -313,9 +377,11 @@ def run_ours(args, view, world, rank, local, dist):
         "plain_mp": plain,
         "perturb_vs_plain": (value / world / plain["value"]) if plain else None,
     }
+    r.close()
+    if args.serve_requests > 0:
+        line["serving"] = run_serving(args, local)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(view, args.cpu_seconds)
-    r.close()
     print(json.dumps(line), flush=True)
 
 

@@ -256,6 +256,110 @@ int mdzgpu_measure_peak(int device, int kind, double* ops_per_s);
  * Used to check the drop-in ABI against MDZ's own headers. */
 int mdzgpu_abi_layout(int64_t* out, int n);
 
+/* ---- Serving engine (new; the reference renders one image at a time) ----
+ *
+ * A server owns one GPU and renders many requests at once.  Requests are
+ * admitted in arrival order while a slot, device memory (`arena_bytes`),
+ * pinned result staging (`staging_bytes`) and work-queue room are free; an
+ * admitted request's pixels join a work queue shared with every other
+ * admitted request of the same method, and each engine step (one CUDA-graph
+ * launch) advances every queued pixel by a bounded number of iterations, so
+ * requests that arrive while others run start at the next step and finish
+ * independently.  Results are bit-identical to rendering the request alone. */
+typedef struct mdzgpu_server mdzgpu_server;
+
+enum {
+    MDZGPU_METHOD_AUTO = 0,       /* perturbation for the Mandelbrot formula,
+                                     multi-limb otherwise */
+    MDZGPU_METHOD_PERTURB = 1,    /* as mdzgpu_render_perturb */
+    MDZGPU_METHOD_MULTI_LIMB = 2  /* multi-limb fixed point, perturbation
+                                     geometry, every formula */
+};
+
+enum {
+    MDZGPU_REQ_QUEUED = 0,
+    MDZGPU_REQ_RUNNING = 1,
+    MDZGPU_REQ_DONE = 2,
+    MDZGPU_REQ_FAILED = 3,
+    MDZGPU_REQ_CANCELLED = 4,
+    MDZGPU_REQ_TIMEOUT = 5
+};
+
+typedef struct mdzgpu_serve_config {
+    int32_t device;
+    int32_t max_requests;         /* admitted at once, 1..64 (0 = 64) */
+    int64_t arena_bytes;          /* device memory for requests (0 = 8 GiB) */
+    int64_t staging_bytes;        /* pinned host memory for results (0 = 512 MiB) */
+    int64_t queue_pixels;         /* pixels in flight per method (0 = 2^24) */
+    double step_ms;               /* target duration of one step (0 = 2 ms) */
+    const char* log_path;         /* JSON line per finished request, or NULL */
+} mdzgpu_serve_config;
+
+/* A render request.  Geometry as mdzgpu_render_perturb: centre (cx, cy),
+ * real-axis width, square pixels.  The mpval limbs are copied by submit.
+ * counts (width*height int32) and mag2 (nullable, float) are host buffers
+ * that must stay valid until the request leaves the RUNNING state. */
+typedef struct mdzgpu_request {
+    int32_t width, height;
+    int32_t family, fractal;      /* MDZ_FAMILY_MANDEL; any MDZ formula */
+    int64_t depth;
+    int64_t precision;
+    mdzgpu_mpval cx, cy, span;
+    int32_t method;               /* MDZGPU_METHOD_* */
+    int32_t pad;
+    double timeout_ms;            /* from submission; 0 = none */
+    int32_t* counts;
+    float* mag2;
+} mdzgpu_request;
+
+typedef struct mdzgpu_request_status {
+    int32_t state;                /* MDZGPU_REQ_* */
+    int32_t error;                /* MDZGPU_ERR_* when FAILED */
+    int32_t method;               /* method used */
+    int32_t words;                /* orbit digits (perturbation) or words */
+    double queue_ms;              /* submission -> admission */
+    double latency_ms;            /* submission -> results in counts */
+    int64_t pixel_iters;          /* sum over pixels of (count ? count : depth) */
+    int64_t escalated_fp64, escalated_mp, rebases;
+    int64_t steps;                /* engine steps the request took part in */
+} mdzgpu_request_status;
+
+typedef struct mdzgpu_serve_stats {
+    int64_t submitted, completed, failed, cancelled, timed_out;
+    int64_t steps;                /* engine steps (graph launches) */
+    int64_t launches;             /* kernels launched by the engine */
+    int64_t pixel_iters;          /* over completed requests */
+    double busy_ms;               /* wall time with work on the GPU */
+    double latency_p50_ms, latency_p99_ms, latency_max_ms;
+    int64_t device_bytes_in_use, device_bytes_peak;
+} mdzgpu_serve_stats;
+
+/* NULL on failure (mdzgpu_last_error). */
+mdzgpu_server* mdzgpu_serve_create(const mdzgpu_serve_config* cfg);
+/* Stops the engine: running requests are cancelled, then everything freed. */
+void mdzgpu_serve_destroy(mdzgpu_server* s);
+/* Queues a request; *id identifies it.  MDZGPU_ERR_NOMEM if it can never fit
+ * the server's memory, MDZGPU_ERR_ARG / _RANGE / _UNSUPPORTED for a bad
+ * request. */
+int mdzgpu_serve_submit(mdzgpu_server* s, const mdzgpu_request* r, int64_t* id);
+/* Current status (any state). */
+int mdzgpu_serve_poll(mdzgpu_server* s, int64_t id, mdzgpu_request_status* out);
+/* Waits until the request leaves QUEUED/RUNNING or timeout_ms passes
+ * (< 0 = no limit); MDZGPU_ERR_TIMEOUT if it did not. */
+int mdzgpu_serve_wait(mdzgpu_server* s, int64_t id, double timeout_ms,
+                      mdzgpu_request_status* out);
+/* Cancels a queued or running request (its buffers are not written after
+ * the call's effect is seen in poll). */
+int mdzgpu_serve_cancel(mdzgpu_server* s, int64_t id);
+/* Forgets a finished request's record (ids of finished requests otherwise
+ * stay pollable). */
+int mdzgpu_serve_release(mdzgpu_server* s, int64_t id);
+int mdzgpu_serve_get_stats(mdzgpu_server* s, mdzgpu_serve_stats* out);
+/* Device and pinned-host bytes a request needs while admitted (no GPU
+ * needed); MDZGPU_ERR_* for a request the server would refuse. */
+int mdzgpu_serve_footprint(const mdzgpu_request* r, int64_t* device_bytes,
+                           int64_t* host_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -534,7 +534,39 @@ constexpr float kLostLimitFp64 = 6.0f;
 
 // Fixed-point pixel coordinates of the perturbation geometry for the
 // multi-limb pass: x[ix] = cx + (2 ix - W) hs, y[line] = cy + (H - 2 line) hs.
-static int perturb_tables(const mdzgpu_mpval* cx, const mdzgpu_mpval* cy, double hs_m, int hs_e,
+}  // extern "C"
+
+namespace mdz {
+
+OrbitLayout orbit_layout(size_t entries, int L)
+{
+    // zf[entries] float2 | zd[entries] double2 | ze[entries] int |
+    // dd[entries] double | de[entries] int | len + progress words |
+    // centre digits | rebases | digits[entries][2][L] int (raw orbit, scratch)
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    OrbitLayout o;
+    o.zd = al(entries * sizeof(float2));
+    o.ze = o.zd + al(entries * sizeof(double2));
+    o.dd = o.ze + al(entries * sizeof(int));
+    o.de = o.dd + al(entries * sizeof(double));
+    o.len = o.de + al(entries * sizeof(int));
+    o.dig = o.len + 256;
+    o.reb = o.dig + al(2 * (size_t)L * sizeof(int));
+    o.raw = o.reb + 256;
+    o.bytes = o.raw + al(entries * 2 * (size_t)L * sizeof(int));
+    return o;
+}
+
+int perturb_mp_words(long precision)
+{
+    const int words = mp_words_for_precision(precision);
+    for (int k = words; k <= mdzgpu_mp_max_words(); ++k)
+        if (mp_words_supported(k))
+            return k;
+    return mdzgpu_mp_max_words();
+}
+
+int perturb_tables(const mdzgpu_mpval* cx, const mdzgpu_mpval* cy, double hs_m, int hs_e,
                           int W, int H, int words, std::vector<uint32_t>& tab)
 {
     std::vector<uint32_t> fcx(words), fcy(words), fhs(words);
@@ -566,6 +598,10 @@ static int perturb_tables(const mdzgpu_mpval* cx, const mdzgpu_mpval* cy, double
     }
     return MDZGPU_OK;
 }
+
+}  // namespace mdz
+
+extern "C" {
 
 static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,
                           const mdzgpu_mpval* cy, const mdzgpu_mpval* width, int64_t precision,
@@ -604,21 +640,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     if ((rc = half_spacing(width, f->width, &hs_m, &hs_e)))
         return rc;
     const size_t n = (size_t)f->width * f->height;
-    const size_t entries = (size_t)f->depth + 2;
-    // orbit layout (256-byte aligned pieces):
-    //   zf[entries] float2 | zd[entries] double2 | ze[entries] int |
-    //   dd[entries] double | de[entries] int | len | centre digits | rebases |
-    //   digits[entries][2][L] int (raw orbit, scratch)
-    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t off_zd = al(entries * sizeof(float2));
-    const size_t off_ze = off_zd + al(entries * sizeof(double2));
-    const size_t off_dd = off_ze + al(entries * sizeof(int));
-    const size_t off_de = off_dd + al(entries * sizeof(double));
-    const size_t off_len = off_de + al(entries * sizeof(int));
-    const size_t off_dig = off_len + 256;
-    const size_t off_reb = off_dig + al(2 * L * sizeof(int));
-    const size_t off_raw = off_reb + 256;
-    const size_t orbit_bytes = off_raw + al(entries * 2 * (size_t)L * sizeof(int));
+    const OrbitLayout ol = orbit_layout((size_t)f->depth + 2, L);
+    const size_t off_zd = ol.zd, off_ze = ol.ze, off_dd = ol.dd, off_de = ol.de;
+    const size_t off_len = ol.len, off_dig = ol.dig, off_reb = ol.reb, off_raw = ol.raw;
+    const size_t orbit_bytes = ol.bytes;
     if ((rc = ctx->orbit.ensure(orbit_bytes)) || (rc = ctx->sync.ensure(sizeof(FrameSync))))
         return rc;
     if (!d_out) {
@@ -727,15 +752,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     }
     // pass 2: the exact multi-limb kernel for what FP64 could not settle
     {
-        const int words = mp_words_for_precision((long)precision);
-        int w = -1;
-        for (int k = words; k <= mdzgpu_mp_max_words(); ++k)
-            if (mp_words_supported(k)) {
-                w = k;
-                break;
-            }
-        if (w < 0)
-            w = mdzgpu_mp_max_words();
+        const int w = perturb_mp_words((long)precision);
         std::vector<uint32_t> tab((size_t)(f->width + f->height + 2) * w, 0);
         if ((rc = perturb_tables(cx, cy, hs_m, hs_e, f->width, f->height, w, tab))) {
             cudaEventDestroy(evo);

@@ -6,6 +6,7 @@
 #include <stdio.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/mdzgpu.h"
 
@@ -123,6 +124,8 @@ struct OrbitLaunch {
     int* de;
     int max_k;              // last index computed (depth + 1)
     int* out_len;           // number of valid entries (device)
+    int* sm_busy = nullptr; // serving: producers per SM id (counted while running)
+    int sm_words = 0;
 };
 int launch_orbit(const OrbitLaunch& p, cudaStream_t s);
 int orbit_max_limbs();
@@ -187,6 +190,19 @@ int mpfr_coordinate_tables(const mdzgpu_mpval* xmin, const mdzgpu_mpval* ymax,
                            int words, uint32_t* xs, uint32_t* ys);
 // A value rounded to p bits (mpfr_set into a p-bit variable), as fixed point.
 int mpfr_round_to_fixed(const mdzgpu_mpval* v, long p, int words, uint32_t* out);
+
+// Reference-orbit buffer: byte offsets of its 256-byte aligned pieces for
+// `entries` entries of L digits (zf at 0).
+struct OrbitLayout {
+    size_t zd, ze, dd, de, len, dig, reb, raw, bytes;
+};
+OrbitLayout orbit_layout(size_t entries, int L);
+// Multi-limb word count of the perturbation's last escalation pass.
+int perturb_mp_words(long precision);
+// Fixed-point pixel coordinates c = centre + ((2 ix - W) hs, (H - 2 line) hs)
+// of the perturbation geometry: tab = [x[W] | y[H]] of `words` words each.
+int perturb_tables(const mdzgpu_mpval* cx, const mdzgpu_mpval* cy, double hs_m, int hs_e,
+                   int W, int H, int words, std::vector<uint32_t>& tab);
 
 
 }  // namespace mdz

@@ -1,5 +1,6 @@
 // Dispatch of the multi-limb kernel by word count.
 #include "internal.h"
+#include "serve.h"
 
 namespace mdz {
 
@@ -23,6 +24,32 @@ int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
 #undef MDZ_CASE
     default:
         set_error("mp kernel: %d words not built", p.words);
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+}
+
+// Class k >= 1 of the serving engine is the k-th word count of the list.
+int serve_mp_class_words(int cls)
+{
+    int k = 0;
+#define MDZ_CASE(n)      \
+    if (++k == cls)      \
+        return n;
+    MDZ_MP_WORDS_LIST(MDZ_CASE)
+#undef MDZ_CASE
+    return 0;
+}
+
+int launch_serve_mp(ServeDev* d, int mp_class, int num_sms, cudaStream_t s)
+{
+    switch (serve_mp_class_words(mp_class)) {
+#define MDZ_CASE(n) \
+    case n:         \
+        return launch_serve_mp_words<n>(d, mp_class, num_sms, s);
+        MDZ_MP_WORDS_LIST(MDZ_CASE)
+#undef MDZ_CASE
+    default:
+        set_error("serve: method class %d has no multi-limb kernel", mp_class);
         return MDZGPU_ERR_UNSUPPORTED;
     }
 }

@@ -18,6 +18,7 @@
 // 8x4 tiles per warp from an atomic counter, as in the FP64 kernel.
 #include "fixed_point.cuh"
 #include "internal.h"
+#include "serve.h"
 
 namespace mdz {
 namespace {
@@ -89,6 +90,63 @@ __device__ __forceinline__ uint32_t escape_mp(uint32_t (&wre)[N], uint32_t (&wim
     }
     mag = fx_top_float<N>(wim2) + fx_top_float<N>(wre2);
     return 0;
+}
+
+// Resumable form for the serving engine: enters with |wre|, |wim| and their
+// sign masks after iteration wz - 1, runs iterations wz .. last (<= depth)
+// with the formula chosen at run time, and returns true when the pixel is
+// finished (count in wz: the escape iteration, or 0 at depth); false leaves
+// the state after iteration `last` (wz = last + 1).  The operations are
+// those of escape_mp, so a pixel split over any number of calls gets the
+// same count.
+template <int N, class CG>
+__device__ __forceinline__ bool escape_mp_resume(uint32_t (&wre)[N], uint32_t (&wim)[N],
+                                                 uint32_t& sre, uint32_t& sim, const CG& c_re,
+                                                 const CG& c_im, int fractal, uint32_t& wz,
+                                                 uint32_t last, uint32_t depth, float& mag)
+{
+    uint32_t wre2[N], wim2[N], acc[N + 2], t[N], d[N];
+    fx::sqr_trunc<N>(wre, acc);
+    fx::extract<N, 24>(acc, wre2);
+    fx::sqr_trunc<N>(wim, acc);
+    fx::extract<N, 24>(acc, wim2);
+    const bool ship = fractal == MDZ_BURNING_SHIP;
+    const bool celtic = fractal == MDZ_GENERALIZED_CELTIC;
+    const bool variant = fractal == MDZ_VARIANT;
+    if (last > depth)
+        last = depth;
+    for (; wz <= last; ++wz) {
+        fx::mul_trunc<N>(wre, wim, acc);
+        fx::extract<N, 23>(acc, t);
+        const uint32_t mt = ship ? 0u : (sre ^ sim);
+        fx::add_signed<N>(c_im, t, mt, wim);
+        fx::sub<N>(wre2, wim2, d);
+        uint32_t md = 0u;
+        if (celtic || (variant && (wz & 1u)))
+            md = (uint32_t)((int32_t)d[N - 1] >> 31);
+        fx::add_signed<N>(c_re, d, md, wre);
+        if (fx::big<N>(wre) || fx::big<N>(wim)) {
+            const float a = fx_top_float<N>(wre), b = fx_top_float<N>(wim);
+            mag = a * a + b * b;
+            return true;
+        }
+        sre = fx::abs_inplace<N>(wre);
+        sim = fx::abs_inplace<N>(wim);
+        fx::sqr_trunc<N>(wim, acc);
+        fx::extract<N, 24>(acc, wim2);
+        fx::sqr_trunc<N>(wre, acc);
+        fx::extract<N, 24>(acc, wre2);
+        if (fx::sum_gt4<N>(wim2, wre2)) {
+            mag = fx_top_float<N>(wim2) + fx_top_float<N>(wre2);
+            return true;
+        }
+    }
+    mag = fx_top_float<N>(wim2) + fx_top_float<N>(wre2);
+    if (wz > depth) {
+        wz = 0;
+        return true;
+    }
+    return false;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
@@ -196,6 +254,131 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
     }
 }
 
+// Serving: one step of the multi-limb method over its mixed work queue
+// (class `cls`); see serve.h.  State per pixel: |wre| (N words), |wim| (N
+// words), the next iteration, the two sign masks.
+template <int N>
+__global__ void __launch_bounds__(block_threads<N>()) serve_mp_kernel(ServeDev* __restrict__ d,
+                                                                     int cls)
+{
+    extern __shared__ uint32_t smem[];
+    if (serve_block_leaves(d, cls))
+        return;
+    const unsigned cur = d->ctl.cur;
+    const unsigned n = d->status.qcount[cls][cur];
+    const unsigned* qin = d->queue[cls][cur];
+    unsigned* qout = d->queue[cls][cur ^ 1u];
+    unsigned* qout_count = &d->status.qcount[cls][cur ^ 1u];
+    const unsigned long long cancel = d->ctl.cancel;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0)
+            base = atomicAdd(&d->qpull[cls], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const unsigned i = base + lane;
+        const bool valid = i < n;
+        const unsigned e = valid ? qin[i] : 0u;
+        const int slot = (int)(e >> kEntrySlotShift);
+        const unsigned pix = e & kEntryPixelMask;
+        bool done = false, again = false;
+        if (valid) {
+            if ((cancel >> slot) & 1ull) {
+                done = true;
+            } else {
+                const ServeReq& rq = d->req[slot];
+                const int W = rq.pl.W;
+                const int line = (int)(pix / (unsigned)W);
+                const int ix = (int)(pix - (unsigned)line * (unsigned)W);
+                const uint32_t* xs = rq.xs + (size_t)ix * N;
+                const uint32_t* ys = rq.ys + (size_t)line * N;
+                uint32_t* sp = (uint32_t*)(rq.state + (size_t)pix * rq.state_stride);
+                uint32_t wre[N], wim[N], sre, sim, wz;
+                if (e & kEntryFresh) {
+#pragma unroll
+                    for (int k = 0; k < N; ++k) {
+                        wre[k] = xs[k];
+                        wim[k] = ys[k];
+                    }
+                    sre = fx::abs_inplace<N>(wre);
+                    sim = fx::abs_inplace<N>(wim);
+                    wz = 1;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < N; ++k) {
+                        wre[k] = sp[k];
+                        wim[k] = sp[N + k];
+                    }
+                    wz = sp[2 * N];
+                    const uint32_t sg = sp[2 * N + 1];
+                    sre = (sg & 1u) ? 0xffffffffu : 0u;
+                    sim = (sg & 2u) ? 0xffffffffu : 0u;
+                }
+                const uint32_t last = wz + d->ctl.budget[slot] - 1u;
+                const uint32_t depth = rq.pl.depth;
+                float mag = 0.f;
+                bool fin;
+                if constexpr (c_in_smem<N>()) {
+                    const int stride = blockDim.x;
+                    uint32_t* cre = smem + threadIdx.x;
+                    uint32_t* cim = smem + (size_t)N * stride + threadIdx.x;
+#pragma unroll
+                    for (int k = 0; k < N; ++k) {
+                        cre[k * stride] = xs[k];
+                        cim[k * stride] = ys[k];
+                    }
+                    CShared<N> gr{cre, stride}, gi{cim, stride};
+                    fin = escape_mp_resume<N>(wre, wim, sre, sim, gr, gi, rq.fractal, wz, last,
+                                              depth, mag);
+                } else {
+                    CRegs<N> gr, gi;
+#pragma unroll
+                    for (int k = 0; k < N; ++k) {
+                        gr.w[k] = xs[k];
+                        gi.w[k] = ys[k];
+                    }
+                    fin = escape_mp_resume<N>(wre, wim, sre, sim, gr, gi, rq.fractal, wz, last,
+                                              depth, mag);
+                }
+                if (fin) {
+                    rq.pl.out[pix] = (int32_t)wz;
+                    if (rq.pl.mag)
+                        rq.pl.mag[pix] = mag;
+                    done = true;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < N; ++k) {
+                        sp[k] = wre[k];
+                        sp[N + k] = wim[k];
+                    }
+                    sp[2 * N] = wz;
+                    sp[2 * N + 1] = (sre & 1u) | (sim & 2u);
+                    again = true;
+                }
+            }
+        }
+        // warp-aggregated append of the unfinished pixels
+        const unsigned amask = __ballot_sync(0xffffffffu, again);
+        if (amask) {
+            const int leader = __ffs(amask) - 1;
+            unsigned b = 0;
+            if (lane == leader)
+                b = atomicAdd(qout_count, (unsigned)__popc(amask));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (again)
+                qout[b + __popc(amask & ((1u << lane) - 1u))] = e & ~kEntryFresh;
+        }
+        const unsigned dmask = __ballot_sync(0xffffffffu, done);
+        if (done) {
+            const unsigned grp = __match_any_sync(dmask, slot);
+            if (lane == __ffs(grp) - 1)
+                atomicSub(d->status.remaining + slot, (unsigned)__popc(grp));
+        }
+    }
+}
+
 template <int N, int FRACTAL, bool JULIA>
 int launch_typed(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
 {
@@ -248,11 +431,33 @@ int launch_words(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
 }
 
 
+template <int N>
+int launch_serve_mp_words(ServeDev* d, int mp_class, int num_sms, cudaStream_t s)
+{
+    constexpr int threads = block_threads<N>();
+    const size_t smem = c_in_smem<N>() ? (size_t)2 * N * threads * sizeof(uint32_t) : 0;
+    static int bps = 0;
+    if (!bps) {
+        if (smem > 48 * 1024)
+            MDZ_CUDA_TRY(cudaFuncSetAttribute(serve_mp_kernel<N>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, serve_mp_kernel<N>,
+                                                                   threads, smem));
+        if (bps < 1)
+            bps = 1;
+    }
+    serve_mp_kernel<N><<<(unsigned)(num_sms * bps), threads, smem, s>>>(d, mp_class);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
 #ifdef MDZ_MP_WORDS
 // One translation unit per word count (the build compiles this file once for
 // every count in the list) keeps the large unrolled kernels compiling in
 // parallel.
 template int launch_words<MDZ_MP_WORDS>(mdzgpu_ctx*, const MpLaunch&, cudaStream_t);
+template int launch_serve_mp_words<MDZ_MP_WORDS>(ServeDev*, int, int, cudaStream_t);
 #endif
 
 }  // namespace mdz

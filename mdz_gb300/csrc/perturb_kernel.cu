@@ -30,6 +30,7 @@
 #include <math.h>
 
 #include "internal.h"
+#include "serve.h"
 
 namespace mdz {
 namespace {
@@ -232,7 +233,18 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
 
 __global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
 {
+    // serving: the slice kernels keep their blocks off an SM while a
+    // producer runs there, so its latency-bound warps own the issue slots
+    unsigned smid = 0;
+    if (p.sm_busy) {
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        smid %= (unsigned)p.sm_words;
+        if (threadIdx.x == 0)
+            atomicAdd(p.sm_busy + smid, 1);
+    }
     orbit_produce(p, nullptr);
+    if (p.sm_busy && threadIdx.x == 0)
+        atomicSub(p.sm_busy + smid, 1);
 }
 
 // Per entry k (one thread each): the FP64 pair with its exponent, the FP32
@@ -522,14 +534,6 @@ __device__ __forceinline__ void load_z(const PerturbLaunch& p, int m, T& zx, T& 
     }
 }
 
-// One pixel.  Returns the count; mag_out gets |z|^2 at escape.  `lost`
-// accumulates the bits cancelled by rebases (log2 |dz| / |z| at each one):
-// a pixel whose deltas lost more than the mantissa can spare is re-run by
-// the next, more precise, pass.
-// In the fused launch (STREAM) the orbit is still being produced: entries
-// below `avail` are finished; a pixel that needs entry m + 1 waits (bounded)
-// for the finisher, and learns the final length K once the producer is done.
-// Returns false when a wait gave up (error flag raised).
 // Per-block copy of the orbit progress: pixel threads read shared memory;
 // one elected thread at a time refreshes it from global memory, so the
 // hundreds of thousands of waiting threads do not hammer one L2 line (which
@@ -577,41 +581,65 @@ __device__ __forceinline__ bool wait_orbit(const PerturbLaunch& p, BlockOrbitVie
     }
 }
 
+// Resumable state of one pixel: the deltas, the reference index m, the next
+// iteration wz, the bits lost to rebases so far.  (s, s2x4, dc 2^-e and the
+// flags follow from t, e and dc, so they are recomputed on resume and a
+// resumed run is bit-identical to an uninterrupted one.)
+template <class T>
+struct PixRun {
+    PixState<T> st;
+    int m;
+    uint32_t wz;
+    float lost;
+    unsigned rebases;
+    float mag;
+};
+
+template <class T>
+__device__ __forceinline__ void pixel_start(PixRun<T>& r, double dcm_r, double dcm_i, int dce)
+{
+    set_from_double(r.st, dcm_r, dcm_i, dce);
+    refresh_scale(r.st, (T)dcm_r, (T)dcm_i, dce);
+    r.m = 1;
+    r.wz = 1;
+    r.lost = 0.f;
+    r.rebases = 0;
+    r.mag = 0.f;
+}
+
+// Iterations r.wz .. wz_last (inclusive, <= depth).  Returns 1 when the
+// pixel is finished (*count = escape iteration, or 0 at depth), 0 when it
+// stopped after wz_last (state in r), -1 when an orbit wait gave up.
 template <class T, bool STREAM>
-__device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
-                                  float& mag_out, unsigned& rebases, float& lost,
-                                  BlockOrbitView* view)
+__device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, double dcm_i,
+                           int dce, uint32_t wz_last, uint32_t& count, BlockOrbitView* view)
 {
     const T dcf_r = (T)dcm_r, dcf_i = (T)dcm_i;
-    PixState<T> st;
-    set_from_double(st, dcm_r, dcm_i, dce);
-    refresh_scale(st, dcf_r, dcf_i, dce);
-    int m = 1;
+    PixState<T>& st = r.st;
+    int m = r.m;
     // entries 0..avail-1 readable; K = orbit length (unknown while streaming)
     int K = STREAM ? 0x7fffffff : *p.orbit_len;
     int avail = K;
-    if (STREAM && !wait_orbit(p, view, 1, avail, K)) {
-        mag_out = 0.f;
-        return 0;
-    }
+    if (STREAM && !wait_orbit(p, view, m, avail, K))
+        return -1;
     T Zx, Zy;
-    load_z<T>(p, 1, Zx, Zy);
+    load_z<T>(p, m, Zx, Zy);
     const T band_lo = (T)4 - (T)6.1035156e-5;  // 4 - 2^-14
     const T band_hi = (T)4 + (T)6.1035156e-5;
-    T magT = (T)0;
-    for (uint32_t wz = 1; wz <= p.depth; ++wz) {
+    T magT = (T)r.mag;
+    const uint32_t last = wz_last < p.depth ? wz_last : p.depth;
+    uint32_t wz = r.wz;
+    for (; wz <= last; ++wz) {
         if (m + 1 >= avail) {
-            if (STREAM && m + 1 < K && !wait_orbit(p, view, m + 1, avail, K)) {
-                mag_out = 0.f;
-                return 0;
-            }
+            if (STREAM && m + 1 < K && !wait_orbit(p, view, m + 1, avail, K))
+                return -1;
             if (m >= K - 1) {
                 // end of the reference orbit: rebase onto Z_0 = 0
-                rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, lost, false);
+                rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, r.lost, false);
                 m = 0;
                 Zx = (T)0;
                 Zy = (T)0;
-                ++rebases;
+                ++r.rebases;
             }
         }
         if (st.careful && (st.force_slow || Zx * Zx + Zy * Zy < (T)Mant<T>::kTinyZ2)) {
@@ -632,8 +660,9 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
         if (magT > band_lo) {
             // within 2^-14 of the bailout the rounded Z_m can not decide it
             if (magT > band_hi || escape_exact<T>(p, m, st)) {
-                mag_out = (float)magT;
-                return wz;
+                r.mag = (float)magT;
+                count = wz;
+                return 1;
             }
         }
         // rebase test |Z_m + dz| < |dz|: it can only hold when
@@ -641,11 +670,11 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
         const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
         const T zn2 = Mant<T>::fma_(Zx, Zx, Zy * Zy);
         if (Mant<T>::fma_(st.s2x4, dd, -zn2) >= (T)0 || zn2 < (T)Mant<T>::kGlitchZ2) {
-            if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, lost, true)) {
+            if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, r.lost, true)) {
                 m = 0;
                 Zx = (T)0;
                 Zy = (T)0;
-                ++rebases;
+                ++r.rebases;
                 continue;
             }
         }
@@ -663,8 +692,37 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
             }
         }
     }
-    mag_out = (float)magT;
+    r.mag = (float)magT;
+    r.m = m;
+    r.wz = wz;
+    if (wz > p.depth) {
+        count = 0;
+        return 1;
+    }
     return 0;
+}
+
+// One pixel.  Returns the count; mag_out gets |z|^2 at escape.  `lost`
+// accumulates the bits cancelled by rebases (log2 |dz| / |z| at each one):
+// a pixel whose deltas lost more than the mantissa can spare is re-run by
+// the next, more precise, pass.
+// In the fused launch (STREAM) the orbit is still being produced: entries
+// below `avail` are finished; a pixel that needs entry m + 1 waits (bounded)
+// for the finisher, and learns the final length K once the producer is done.
+// A wait that gives up raises the error flag and leaves the count 0.
+template <class T, bool STREAM>
+__device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
+                                  float& mag_out, unsigned& rebases, float& lost,
+                                  BlockOrbitView* view)
+{
+    PixRun<T> r;
+    pixel_start(r, dcm_r, dcm_i, dce);
+    uint32_t count = 0;
+    const int done = perturb_run<T, STREAM>(p, r, dcm_r, dcm_i, dce, p.depth, count, view);
+    mag_out = r.mag;
+    rebases += r.rebases;
+    lost += r.lost;
+    return done == 1 ? count : 0;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
@@ -795,7 +853,180 @@ __global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, Pe
     pixel_tiles<float, WANT_MAG, false, true>(p);
 }
 
+// ---- serving: one step of the FP32 pass over a mixed work queue ----
+
+// 32 bytes of resumable state per pixel (two uint4).
+__device__ __forceinline__ void store_run(const PixRun<float>& r, uint4* sp)
+{
+    sp[0] = make_uint4(__float_as_uint(r.st.tr), __float_as_uint(r.st.ti), (unsigned)r.st.e,
+                       (unsigned)r.m);
+    sp[1] = make_uint4(r.wz, __float_as_uint(r.lost), __float_as_uint(r.mag), r.rebases);
+}
+
+__device__ __forceinline__ void load_run(PixRun<float>& r, const uint4* sp, double dcm_r,
+                                         double dcm_i, int dce)
+{
+    const uint4 a = sp[0], b = sp[1];
+    r.st.tr = __uint_as_float(a.x);
+    r.st.ti = __uint_as_float(a.y);
+    r.st.e = (int)a.z;
+    r.m = (int)a.w;
+    r.wz = b.x;
+    r.lost = __uint_as_float(b.y);
+    r.mag = __uint_as_float(b.z);
+    r.rebases = b.w;
+    refresh_scale(r.st, (float)dcm_r, (float)dcm_i, dce);
+}
+
+// Warp-aggregated append of the lanes with `want` set to a queue.
+__device__ __forceinline__ void queue_append(bool want, unsigned value, unsigned* q,
+                                             unsigned* count)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (!mask)
+        return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if (lane == leader)
+        base = atomicAdd(count, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (want)
+        q[base + __popc(mask & ((1u << lane) - 1u))] = value;
+}
+
+// Lanes with `done` set subtract one each from remaining[slot], one atomic
+// per distinct slot in the warp.
+__device__ __forceinline__ void retire_pixels(bool done, int slot, unsigned* remaining)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, done);
+    if (!done)
+        return;
+    const unsigned grp = __match_any_sync(mask, slot);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1)
+        atomicSub(remaining + slot, (unsigned)__popc(grp));
+}
+
+__global__ void __launch_bounds__(256, 5) serve_perturb_kernel(ServeDev* __restrict__ d)
+{
+    if (serve_block_leaves(d, 0))
+        return;
+    const unsigned cur = d->ctl.cur;
+    const unsigned n = d->status.qcount[0][cur];
+    const unsigned* qin = d->queue[0][cur];
+    unsigned* qout = d->queue[0][cur ^ 1u];
+    unsigned* qout_count = &d->status.qcount[0][cur ^ 1u];
+    const unsigned long long cancel = d->ctl.cancel;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0)
+            base = atomicAdd(&d->qpull[0], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const unsigned i = base + lane;
+        const bool valid = i < n;
+        const unsigned e = valid ? qin[i] : 0u;
+        const int slot = (int)(e >> kEntrySlotShift);
+        const unsigned pix = e & kEntryPixelMask;
+        bool done = false, again = false;
+        if (valid) {
+            if ((cancel >> slot) & 1ull) {
+                done = true;
+            } else {
+                const ServeReq& rq = d->req[slot];
+                const PerturbLaunch& p = rq.pl;
+                const int line = (int)(pix / (unsigned)p.W);
+                const int ix = (int)(pix - (unsigned)line * (unsigned)p.W);
+                const double dcm_r = (double)(2 * ix - p.W) * p.hs_m;
+                const double dcm_i = (double)(p.H - 2 * line) * p.hs_m;
+                uint4* sp = rq.state + (size_t)pix * 2u;
+                PixRun<float> r;
+                if (e & kEntryFresh)
+                    pixel_start(r, dcm_r, dcm_i, p.hs_e);
+                else
+                    load_run(r, sp, dcm_r, dcm_i, p.hs_e);
+                const uint32_t last = r.wz + d->ctl.budget[slot] - 1u;
+                uint32_t count = 0;
+                if (perturb_run<float, false>(p, r, dcm_r, dcm_i, p.hs_e, last, count, nullptr)
+                    == 1) {
+                    p.out[pix] = (int32_t)count;
+                    if (p.mag)
+                        p.mag[pix] = r.mag;
+                    if (r.lost > p.lost_limit && p.flag_out)
+                        p.flag_out[atomicAdd(p.flag_out_count, 1u)] = pix;
+                    if (r.rebases)
+                        atomicAdd(p.rebases, (unsigned long long)r.rebases);
+                    done = true;
+                } else {
+                    store_run(r, sp);
+                    again = true;
+                }
+            }
+        }
+        queue_append(again, e & ~kEntryFresh, qout, qout_count);
+        retire_pixels(done, slot, d->status.remaining);
+    }
+}
+
+__global__ void serve_enqueue_kernel(ServeDev* d, int cls, int q, int slot, unsigned npix)
+{
+    unsigned* queue = d->queue[cls][q];
+    const unsigned base = d->status.qcount[cls][q];
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x)
+        queue[base + i] = serve_entry(slot, true, i);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        d->status.remaining[slot] = npix;
+}
+
+__global__ void serve_enqueue_count_kernel(ServeDev* d, int cls, int q, unsigned npix)
+{
+    d->status.qcount[cls][q] += npix;
+}
+
+__global__ void serve_step_end_kernel(ServeDev* d)
+{
+    const unsigned cur = d->ctl.cur;
+    for (int c = threadIdx.x; c < kServeClasses; c += blockDim.x) {
+        d->status.qcount[c][cur] = 0u;
+        d->qpull[c] = 0u;
+        d->qworkers[c] = 0u;
+    }
+}
+
 }  // namespace
+
+int launch_serve_perturb(ServeDev* d, int num_sms, cudaStream_t s)
+{
+    static int bps = 0;
+    if (!bps) {
+        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, serve_perturb_kernel,
+                                                                   256, 0));
+        if (bps < 1)
+            bps = 1;
+    }
+    serve_perturb_kernel<<<(unsigned)(num_sms * bps), 256, 0, s>>>(d);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
+int launch_serve_enqueue(ServeDev* d, int cls, int q, int slot, unsigned npix, cudaStream_t s)
+{
+    const unsigned blocks = npix ? (npix + 255u) / 256u : 1u;
+    serve_enqueue_kernel<<<blocks < 1024u ? blocks : 1024u, 256, 0, s>>>(d, cls, q, slot, npix);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    serve_enqueue_count_kernel<<<1, 1, 0, s>>>(d, cls, q, npix);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
+int launch_serve_step_end(ServeDev* d, cudaStream_t s)
+{
+    serve_step_end_kernel<<<1, 32, 0, s>>>(d);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
 
 int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
 {

@@ -1,0 +1,1227 @@
+// Serving engine, host side: request preparation, admission by memory
+// footprint, the step loop (one CUDA-graph launch per step) and completion.
+//
+// Life of a request:
+//   submit (caller's thread): validate, compute the orbit centre digits or
+//     the fixed-point pixel coordinates, footprint; queue it.
+//   admit (engine thread, arrival order): a slot, a piece of the device arena,
+//     a piece of the pinned staging arena and work-queue room; copy the
+//     inputs; perturbation: launch its reference orbit on the slot's
+//     high-priority stream (the orbit runs beside the steps of other
+//     requests); multi-limb: enqueue its pixels.
+//   orbit finished -> enqueue its pixels.
+//   steps: every queued pixel of every request advances by at most its
+//     request's budget of iterations (budgets give each running request an
+//     equal share of the step).
+//   all pixels finished -> perturbation: the FP64 and multi-limb
+//     escalation passes over the flagged pixels on the slot's stream; then
+//     the results are copied to pinned staging, then to the caller's
+//     buffers; the request's memory is released.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "internal.h"
+#include "serve.h"
+
+namespace mdz {
+namespace {
+
+double wall_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+constexpr size_t kAlign = 256;
+inline size_t al(size_t b)
+{
+    return (b + kAlign - 1) & ~(kAlign - 1);
+}
+
+// First-fit allocator of byte ranges in [0, size), 256-byte granules,
+// neighbouring free ranges merged on release.
+class Arena {
+public:
+    void reset(size_t size)
+    {
+        size_ = size;
+        used_ = 0;
+        free_.clear();
+        if (size)
+            free_[0] = size;
+    }
+    bool alloc(size_t bytes, size_t* off)
+    {
+        bytes = al(bytes ? bytes : 1);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < bytes)
+                continue;
+            *off = it->first;
+            const size_t rest = it->second - bytes, at = it->first + bytes;
+            free_.erase(it);
+            if (rest)
+                free_[at] = rest;
+            used_ += bytes;
+            return true;
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes)
+    {
+        bytes = al(bytes ? bytes : 1);
+        used_ -= bytes;
+        auto next = free_.lower_bound(off);
+        if (next != free_.end() && off + bytes == next->first) {
+            bytes += next->second;
+            next = free_.erase(next);
+        }
+        if (next != free_.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == off) {
+                prev->second += bytes;
+                return;
+            }
+        }
+        free_[off] = bytes;
+    }
+    size_t size() const { return size_; }
+    size_t used() const { return used_; }
+
+private:
+    size_t size_ = 0, used_ = 0;
+    std::map<size_t, size_t> free_;
+};
+
+enum Phase { kQueued, kOrbit, kRunning, kFinishing, kEnded };
+
+// Offsets of a request's pieces in its device block and its pinned block.
+struct Layout {
+    size_t counts, mag, state, lists, sync, orbit, tables, dev_bytes;
+    size_t h_tables, h_digits, h_counts, h_mag, h_misc, host_bytes;
+    OrbitLayout ol;
+};
+
+struct Req {
+    int64_t id = 0;
+    int W = 0, H = 0, fractal = 0;
+    uint32_t depth = 0;
+    long precision = 0;
+    int method = 0;        // MDZGPU_METHOD_PERTURB / _MULTI_LIMB
+    int cls = 0;           // work-queue class
+    int words = 0;         // multi-limb words (perturbation: escalation pass)
+    int limbs = 0;         // orbit digits (perturbation)
+    size_t npix = 0;
+    bool want_mag = false;
+    int32_t* out_counts = nullptr;
+    float* out_mag = nullptr;
+    double timeout_ms = 0;
+    std::vector<int> digits;
+    double hs_m = 0;
+    int hs_e = 0;
+    std::vector<uint32_t> tables;
+    Layout lay{};
+    size_t dev_off = 0, host_off = 0;
+    int slot = -1;
+    Phase phase = kQueued;
+    // public status (guarded by the server mutex)
+    int state = MDZGPU_REQ_QUEUED;
+    int error = 0;
+    bool cancel = false;
+    int cancel_state = MDZGPU_REQ_CANCELLED;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int64_t pixel_iters = 0, esc_fp64 = 0, esc_mp = 0, rebases = 0, steps = 0;
+    cudaEvent_t ev_orbit = nullptr, ev_done = nullptr;
+};
+
+Layout make_layout(const Req& r)
+{
+    Layout l{};
+    const size_t n = r.npix;
+    size_t o = 0;
+    l.counts = o;
+    o += al(n * 4);
+    l.mag = o;
+    if (r.want_mag)
+        o += al(n * 4);
+    l.state = o;
+    if (r.method == MDZGPU_METHOD_PERTURB)
+        o += al(n * 32);
+    else
+        o += al(n * (size_t)serve_mp_state_stride(r.words) * 16);
+    l.lists = o;
+    if (r.method == MDZGPU_METHOD_PERTURB)
+        o += al(256 + 2 * n * 4);
+    l.sync = o;
+    o += 256;
+    l.orbit = o;
+    if (r.method == MDZGPU_METHOD_PERTURB) {
+        l.ol = orbit_layout((size_t)r.depth + 2, r.limbs);
+        o += al(l.ol.bytes);
+    }
+    l.tables = o;
+    o += al((size_t)(r.W + r.H) * r.words * 4);
+    l.dev_bytes = o;
+    size_t h = 0;
+    l.h_tables = h;
+    h += al((size_t)(r.W + r.H) * r.words * 4);
+    l.h_digits = h;
+    h += al(2 * (size_t)r.limbs * 4 + 4);
+    l.h_counts = h;
+    h += al(n * 4);
+    l.h_mag = h;
+    if (r.want_mag)
+        h += al(n * 4);
+    l.h_misc = h;
+    h += 256;
+    l.host_bytes = h;
+    return l;
+}
+
+// Validates a request and computes everything the GPU will need.
+int prepare(const mdzgpu_request* q, Req& r)
+{
+    if (!q) {
+        set_error("serve: null request");
+        return MDZGPU_ERR_ARG;
+    }
+    if (q->width <= 0 || q->height <= 0
+        || (long)q->width * q->height > kServeMaxPixels) {
+        set_error("serve: %d x %d pixels outside (0, %ld]", q->width, q->height,
+                  kServeMaxPixels);
+        return MDZGPU_ERR_ARG;
+    }
+    if (q->depth < 1 || q->depth > 0x7ffffffeLL) {
+        set_error("serve: depth %lld outside [1, 2^31 - 2]", (long long)q->depth);
+        return MDZGPU_ERR_ARG;
+    }
+    if (q->family != MDZ_FAMILY_MANDEL) {
+        set_error("serve: only the Mandelbrot family is served");
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    if (q->fractal < MDZ_MANDELBROT || q->fractal > MDZ_VARIANT) {
+        set_error("serve: unknown formula %d", q->fractal);
+        return MDZGPU_ERR_ARG;
+    }
+    if (q->precision < 1 || q->precision > 1 << 20) {
+        set_error("serve: precision %lld", (long long)q->precision);
+        return MDZGPU_ERR_ARG;
+    }
+    int method = q->method;
+    if (method == MDZGPU_METHOD_AUTO)
+        method = q->fractal == MDZ_MANDELBROT ? MDZGPU_METHOD_PERTURB : MDZGPU_METHOD_MULTI_LIMB;
+    if (method != MDZGPU_METHOD_PERTURB && method != MDZGPU_METHOD_MULTI_LIMB) {
+        set_error("serve: unknown method %d", q->method);
+        return MDZGPU_ERR_ARG;
+    }
+    if (method == MDZGPU_METHOD_PERTURB && q->fractal != MDZ_MANDELBROT) {
+        set_error("serve: perturbation is implemented for the Mandelbrot formula only");
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    if (!q->counts) {
+        set_error("serve: null counts buffer");
+        return MDZGPU_ERR_ARG;
+    }
+    r.W = q->width;
+    r.H = q->height;
+    r.fractal = q->fractal;
+    r.depth = (uint32_t)q->depth;
+    r.precision = (long)q->precision;
+    r.method = method;
+    r.npix = (size_t)q->width * q->height;
+    r.want_mag = q->mag2 != nullptr;
+    r.out_counts = q->counts;
+    r.out_mag = q->mag2;
+    r.timeout_ms = q->timeout_ms;
+    const int w_need = mp_words_for_precision(r.precision);
+    r.words = perturb_mp_words(r.precision);
+    if (method == MDZGPU_METHOD_MULTI_LIMB && w_need > mdzgpu_mp_max_words()) {
+        set_error("serve: precision %ld needs %d words, the multi-limb kernel has %d",
+                  r.precision, w_need, mdzgpu_mp_max_words());
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    if (method == MDZGPU_METHOD_PERTURB) {
+        r.cls = 0;
+        r.limbs = mdzgpu_perturb_limbs(r.precision);
+        if (r.limbs < 5 || r.limbs > orbit_max_limbs()) {
+            set_error("serve: %d orbit digits outside [5, %d]", r.limbs, orbit_max_limbs());
+            return MDZGPU_ERR_UNSUPPORTED;
+        }
+        r.digits.assign(2 * (size_t)r.limbs, 0);
+        if (digits28_from_mpval(&q->cx, r.limbs, r.digits.data())
+            || digits28_from_mpval(&q->cy, r.limbs, r.digits.data() + r.limbs)
+            || abs(r.digits[r.limbs - 1]) >= 4 || abs(r.digits[2 * r.limbs - 1]) >= 4) {
+            set_error("serve: centre must satisfy |cx|, |cy| < 4");
+            return MDZGPU_ERR_RANGE;
+        }
+    } else {
+        r.cls = 0;
+        for (int c = 1; c < kServeClasses; ++c)
+            if (serve_mp_class_words(c) == r.words)
+                r.cls = c;
+        if (!r.cls) {
+            set_error("serve: no multi-limb class for %d words", r.words);
+            return MDZGPU_ERR_UNSUPPORTED;
+        }
+    }
+    int rc = half_spacing(&q->span, r.W, &r.hs_m, &r.hs_e);
+    if (rc)
+        return rc;
+    r.tables.assign((size_t)(r.W + r.H) * r.words, 0);
+    if (perturb_tables(&q->cx, &q->cy, r.hs_m, r.hs_e, r.W, r.H, r.words, r.tables)) {
+        set_error("serve: pixel coordinates must satisfy |x|, |y| < 4");
+        return MDZGPU_ERR_RANGE;
+    }
+    r.lay = make_layout(r);
+    return MDZGPU_OK;
+}
+
+// Throughput guesses (pixel-iterations/s on the whole GPU) that turn a step
+// duration into per-request budgets.
+double class_rate(int cls)
+{
+    if (cls == 0)
+        return 3.0e11;
+    const double w = (double)serve_mp_class_words(cls);
+    return 2.0e9 * (34.0 / w) * (34.0 / w);
+}
+
+const char* formula_name(int f)
+{
+    switch (f) {
+    case MDZ_MANDELBROT: return "mandelbrot";
+    case MDZ_BURNING_SHIP: return "burning_ship";
+    case MDZ_GENERALIZED_CELTIC: return "generalized_celtic";
+    case MDZ_VARIANT: return "variant";
+    default: return "unknown";
+    }
+}
+
+}  // namespace
+
+struct Server {
+    mdzgpu_serve_config cfg{};
+    int device = 0, num_sms = 0;
+    cudaStream_t main = nullptr;
+    cudaStream_t side[kServeSlots] = {};
+    cudaStream_t branch[kServeClasses] = {};
+    cudaEvent_t fork = nullptr, join[kServeClasses] = {};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t step_exec = nullptr;
+    ServeDev* d = nullptr;
+    ServeCtl* ctl_h = nullptr;
+    ServeStatus* status_h = nullptr;
+    ServeReq* req_h = nullptr;
+    unsigned* queues = nullptr;
+    char* arena_dev = nullptr;
+    char* stage_host = nullptr;
+    Arena arena, stage;
+    unsigned cur = 0;
+    long qhost[kServeClasses] = {};      // entries in queue `cur`
+    long inflight[kServeClasses] = {};   // admitted pixels per class
+    std::shared_ptr<Req> slots[kServeSlots];
+    int launches_per_step = 0;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Req>> waiting;
+    std::unordered_map<int64_t, std::shared_ptr<Req>> all;
+    int64_t next_id = 1;
+    bool quit = false;
+    std::thread th;
+    // statistics (guarded by mu)
+    mdzgpu_serve_stats st{};
+    std::vector<double> latencies;
+    FILE* log = nullptr;
+
+    int init(const mdzgpu_serve_config* c);
+    void teardown();
+    void run();
+    int capture_step();
+    void admit();
+    int setup(const std::shared_ptr<Req>& r);
+    void poll_orbits();
+    int step();
+    int start_finish(const std::shared_ptr<Req>& r);
+    void poll_finishing();
+    void end(const std::shared_ptr<Req>& r, int state, int error);
+    void check_cancels();
+    int active() const
+    {
+        int n = 0;
+        for (const auto& s : slots)
+            n += s != nullptr;
+        return n;
+    }
+};
+
+int Server::init(const mdzgpu_serve_config* c)
+{
+    if (c)
+        cfg = *c;
+    if (cfg.max_requests <= 0 || cfg.max_requests > kServeSlots)
+        cfg.max_requests = kServeSlots;
+    if (cfg.arena_bytes <= 0)
+        cfg.arena_bytes = 8LL << 30;
+    if (cfg.staging_bytes <= 0)
+        cfg.staging_bytes = 512LL << 20;
+    if (cfg.queue_pixels <= 0)
+        cfg.queue_pixels = 1LL << 23;
+    if (cfg.queue_pixels > kServeMaxPixels)
+        cfg.queue_pixels = kServeMaxPixels;
+    if (cfg.step_ms <= 0)
+        cfg.step_ms = 2.0;
+    device = cfg.device;
+    MDZ_CUDA_TRY(cudaSetDevice(device));
+    MDZ_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
+    int lo = 0, hi = 0;
+    MDZ_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    MDZ_CUDA_TRY(cudaStreamCreateWithFlags(&main, cudaStreamNonBlocking));
+    for (auto& s : side)
+        MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi));
+    for (auto& s : branch)
+        MDZ_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    MDZ_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    for (auto& e : join)
+        MDZ_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    MDZ_CUDA_TRY(cudaMalloc((void**)&d, sizeof(ServeDev)));
+    MDZ_CUDA_TRY(cudaMemset(d, 0, sizeof(ServeDev)));
+    MDZ_CUDA_TRY(cudaHostAlloc((void**)&ctl_h, sizeof(ServeCtl), cudaHostAllocDefault));
+    MDZ_CUDA_TRY(cudaHostAlloc((void**)&status_h, sizeof(ServeStatus), cudaHostAllocDefault));
+    MDZ_CUDA_TRY(cudaHostAlloc((void**)&req_h, sizeof(ServeReq) * kServeSlots,
+                               cudaHostAllocDefault));
+    memset(ctl_h, 0, sizeof(ServeCtl));
+    memset(status_h, 0, sizeof(ServeStatus));
+    memset((void*)req_h, 0, sizeof(ServeReq) * kServeSlots);
+    const size_t qbytes = (size_t)cfg.queue_pixels * 4;
+    MDZ_CUDA_TRY(cudaMalloc((void**)&queues, qbytes * 2 * kServeClasses));
+    {
+        unsigned* qptr[kServeClasses][2];
+        for (int c = 0; c < kServeClasses; ++c)
+            for (int k = 0; k < 2; ++k)
+                qptr[c][k] = queues + ((size_t)c * 2 + k) * (size_t)cfg.queue_pixels;
+        MDZ_CUDA_TRY(cudaMemcpy(&d->queue[0][0], qptr, sizeof qptr, cudaMemcpyHostToDevice));
+    }
+    MDZ_CUDA_TRY(cudaMalloc((void**)&arena_dev, (size_t)cfg.arena_bytes));
+    MDZ_CUDA_TRY(cudaHostAlloc((void**)&stage_host, (size_t)cfg.staging_bytes,
+                               cudaHostAllocDefault));
+    arena.reset((size_t)cfg.arena_bytes);
+    stage.reset((size_t)cfg.staging_bytes);
+    // one direct launch of every kernel (queues empty: they exit at once)
+    // sets their launch attributes outside the capture
+    int rc = launch_serve_perturb(d, num_sms, main);
+    for (int c = 1; !rc && c < kServeClasses; ++c)
+        rc = launch_serve_mp(d, c, num_sms, main);
+    if (!rc)
+        rc = launch_serve_step_end(d, main);
+    if (rc)
+        return rc;
+    MDZ_CUDA_TRY(cudaStreamSynchronize(main));
+    if ((rc = capture_step()))
+        return rc;
+    if (cfg.log_path && cfg.log_path[0]) {
+        log = fopen(cfg.log_path, "a");
+        if (!log) {
+            set_error("serve: cannot open log %s", cfg.log_path);
+            return MDZGPU_ERR_ARG;
+        }
+    }
+    th = std::thread([this] { run(); });
+    return MDZGPU_OK;
+}
+
+// One step as a graph: control block in, every method's slice kernel in
+// parallel branches, queue flip, status out.
+int Server::capture_step()
+{
+    MDZ_CUDA_TRY(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal));
+    int rc = MDZGPU_OK;
+    launches_per_step = 0;
+    if (cudaMemcpyAsync(&d->ctl, ctl_h, sizeof(ServeCtl), cudaMemcpyHostToDevice, main)
+        != cudaSuccess
+        || cudaEventRecord(fork, main) != cudaSuccess)
+        rc = MDZGPU_ERR_CUDA;
+    for (int c = 0; !rc && c < kServeClasses; ++c) {
+        if (cudaStreamWaitEvent(branch[c], fork, 0) != cudaSuccess) {
+            rc = MDZGPU_ERR_CUDA;
+            break;
+        }
+        rc = c == 0 ? launch_serve_perturb(d, num_sms, branch[c])
+                    : launch_serve_mp(d, c, num_sms, branch[c]);
+        ++launches_per_step;
+        if (!rc && (cudaEventRecord(join[c], branch[c]) != cudaSuccess
+                    || cudaStreamWaitEvent(main, join[c], 0) != cudaSuccess))
+            rc = MDZGPU_ERR_CUDA;
+    }
+    if (!rc) {
+        rc = launch_serve_step_end(d, main);
+        ++launches_per_step;
+    }
+    if (!rc && cudaMemcpyAsync(status_h, &d->status, sizeof(ServeStatus), cudaMemcpyDeviceToHost,
+                               main) != cudaSuccess)
+        rc = MDZGPU_ERR_CUDA;
+    const cudaError_t e = cudaStreamEndCapture(main, &graph);
+    if (rc) {
+        set_error("serve: step capture failed");
+        return rc;
+    }
+    MDZ_CUDA_TRY(e);
+    MDZ_CUDA_TRY(cudaGraphInstantiate(&step_exec, graph, 0));
+    return MDZGPU_OK;
+}
+
+void Server::end(const std::shared_ptr<Req>& r, int state, int error)
+{
+    if (r->slot >= 0) {
+        arena.release(r->dev_off, r->lay.dev_bytes);
+        stage.release(r->host_off, r->lay.host_bytes);
+        inflight[r->cls] -= (long)r->npix;
+        slots[r->slot] = nullptr;
+        r->slot = -1;
+    }
+    if (r->ev_orbit)
+        cudaEventDestroy(r->ev_orbit);
+    if (r->ev_done)
+        cudaEventDestroy(r->ev_done);
+    r->ev_orbit = r->ev_done = nullptr;
+    r->phase = kEnded;
+    std::lock_guard<std::mutex> lk(mu);
+    r->state = state;
+    r->error = error;
+    r->t_done = wall_ms();
+    if (state == MDZGPU_REQ_DONE) {
+        st.completed++;
+        st.pixel_iters += r->pixel_iters;
+        latencies.push_back(r->t_done - r->t_submit);
+        if (log) {
+            const double lat = r->t_done - r->t_submit;
+            fprintf(log,
+                    "{\"id\": %lld, \"width\": %d, \"height\": %d, \"precision\": %ld, "
+                    "\"formula\": \"%s\", \"depth\": %u, \"method\": \"%s\", \"words\": %d, "
+                    "\"pixel_iters\": %lld, \"queue_ms\": %.3f, \"latency_ms\": %.3f, "
+                    "\"pixel_iters_per_s\": %.6g, \"escalated_fp64\": %lld, "
+                    "\"escalated_mp\": %lld, \"steps\": %lld}\n",
+                    (long long)r->id, r->W, r->H, r->precision, formula_name(r->fractal),
+                    r->depth, r->method == MDZGPU_METHOD_PERTURB ? "perturbation" : "multi_limb",
+                    r->method == MDZGPU_METHOD_PERTURB ? r->limbs : r->words,
+                    (long long)r->pixel_iters, r->t_admit - r->t_submit, lat,
+                    lat > 0 ? (double)r->pixel_iters / (lat * 1e-3) : 0.0,
+                    (long long)r->esc_fp64, (long long)r->esc_mp, (long long)r->steps);
+            fflush(log);
+        }
+    } else if (state == MDZGPU_REQ_FAILED) {
+        st.failed++;
+    } else if (state == MDZGPU_REQ_TIMEOUT) {
+        st.timed_out++;
+    } else {
+        st.cancelled++;
+    }
+    cv_done.notify_all();
+}
+
+void Server::check_cancels()
+{
+    const double now = wall_ms();
+    std::vector<std::shared_ptr<Req>> drop;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto it = waiting.begin(); it != waiting.end();) {
+            auto& r = *it;
+            if (!r->cancel && r->timeout_ms > 0 && now - r->t_submit > r->timeout_ms) {
+                r->cancel = true;
+                r->cancel_state = MDZGPU_REQ_TIMEOUT;
+            }
+            if (r->cancel) {
+                drop.push_back(r);
+                it = waiting.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        for (auto& s : slots)
+            if (s && !s->cancel && s->timeout_ms > 0 && now - s->t_submit > s->timeout_ms
+                && s->phase != kFinishing) {
+                s->cancel = true;
+                s->cancel_state = MDZGPU_REQ_TIMEOUT;
+            }
+    }
+    for (auto& r : drop)
+        end(r, r->cancel_state, 0);
+}
+
+void Server::admit()
+{
+    for (;;) {
+        std::shared_ptr<Req> r;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (waiting.empty())
+                return;
+            r = waiting.front();
+        }
+        int slot = -1;
+        for (int s = 0; s < cfg.max_requests; ++s)
+            if (!slots[s]) {
+                slot = s;
+                break;
+            }
+        if (slot < 0 || inflight[r->cls] + (long)r->npix > cfg.queue_pixels)
+            return;
+        size_t doff = 0, hoff = 0;
+        if (!arena.alloc(r->lay.dev_bytes, &doff))
+            return;
+        if (!stage.alloc(r->lay.host_bytes, &hoff)) {
+            arena.release(doff, r->lay.dev_bytes);
+            return;
+        }
+        r->dev_off = doff;
+        r->host_off = hoff;
+        r->slot = slot;
+        slots[slot] = r;
+        inflight[r->cls] += (long)r->npix;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            waiting.pop_front();
+            r->state = MDZGPU_REQ_RUNNING;
+            r->t_admit = wall_ms();
+            const int64_t used = (int64_t)arena.used();
+            st.device_bytes_in_use = used;
+            st.device_bytes_peak = std::max(st.device_bytes_peak, used);
+        }
+        const int rc = setup(r);
+        if (rc)
+            end(r, MDZGPU_REQ_FAILED, rc);
+    }
+}
+
+int Server::setup(const std::shared_ptr<Req>& r)
+{
+    const Layout& l = r->lay;
+    char* db = arena_dev + r->dev_off;
+    char* hb = stage_host + r->host_off;
+    memcpy(hb + l.h_tables, r->tables.data(), r->tables.size() * 4);
+    MDZ_CUDA_TRY(cudaMemcpyAsync(db + l.tables, hb + l.h_tables, r->tables.size() * 4,
+                                 cudaMemcpyHostToDevice, main));
+    MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, main));
+    ServeReq& q = req_h[r->slot];
+    memset((void*)&q, 0, sizeof q);
+    PerturbLaunch& p = q.pl;
+    p = PerturbLaunch{};
+    p.W = r->W;
+    p.H = r->H;
+    p.row0 = 0;
+    p.nrows = r->H;
+    p.depth = r->depth;
+    p.hs_m = r->hs_m;
+    p.hs_e = r->hs_e;
+    p.out = (int32_t*)(db + l.counts);
+    p.mag = r->want_mag ? (float*)(db + l.mag) : nullptr;
+    p.sync = (FrameSync*)(db + l.sync);
+    q.xs = (const uint32_t*)(db + l.tables);
+    q.ys = q.xs + (size_t)r->W * r->words;
+    q.fractal = r->fractal;
+    q.words = r->words;
+    q.state = (uint4*)(db + l.state);
+    if (r->method == MDZGPU_METHOD_PERTURB) {
+        char* ob = db + l.orbit;
+        const OrbitLayout& ol = l.ol;
+        memcpy(hb + l.h_digits, r->digits.data(), r->digits.size() * 4);
+        MDZ_CUDA_TRY(cudaMemcpyAsync(ob + ol.dig, hb + l.h_digits, r->digits.size() * 4,
+                                     cudaMemcpyHostToDevice, main));
+        MDZ_CUDA_TRY(cudaMemsetAsync(ob + ol.len, 0, 256, main));
+        MDZ_CUDA_TRY(cudaMemsetAsync(ob + ol.reb, 0, 256, main));
+        MDZ_CUDA_TRY(cudaMemsetAsync(db + l.lists, 0, 256, main));
+        p.zf = (const float2*)ob;
+        p.zd = (const double2*)(ob + ol.zd);
+        p.ze = (const int*)(ob + ol.ze);
+        p.dd = (const double*)(ob + ol.dd);
+        p.de = (const int*)(ob + ol.de);
+        p.orbit_len = (const int*)(ob + ol.len);
+        p.rebases = (unsigned long long*)(ob + ol.reb);
+        p.lost_limit = 1.0f;  // bits a pixel may lose before its FP64 re-run
+        p.flag_out = (unsigned*)(db + l.lists + 256);
+        p.flag_out_count = (unsigned*)(db + l.lists);
+        q.state_stride = 2;
+        MDZ_CUDA_TRY(cudaMemcpyAsync(&d->req[r->slot], &q, sizeof q, cudaMemcpyHostToDevice,
+                                     main));
+        OrbitLaunch o;
+        o.limbs = r->limbs;
+        o.c_re = (const int*)(ob + ol.dig);
+        o.c_im = o.c_re + r->limbs;
+        o.zf = (float2*)ob;
+        o.zd = (double2*)(ob + ol.zd);
+        o.ze = (int*)(ob + ol.ze);
+        o.dd = (double*)(ob + ol.dd);
+        o.de = (int*)(ob + ol.de);
+        o.digits = (int*)(ob + ol.raw);
+        o.max_k = (int)r->depth + 1;
+        o.out_len = (int*)(ob + ol.len);
+        o.sm_busy = d->sm_busy;
+        o.sm_words = kServeSmWords;
+        cudaEvent_t ready;
+        MDZ_CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+        cudaEventRecord(ready, main);
+        cudaStreamWaitEvent(side[r->slot], ready, 0);
+        cudaEventDestroy(ready);
+        int rc = launch_orbit(o, side[r->slot]);
+        if (rc)
+            return rc;
+        MDZ_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_orbit, cudaEventDisableTiming));
+        MDZ_CUDA_TRY(cudaEventRecord(r->ev_orbit, side[r->slot]));
+        r->phase = kOrbit;
+    } else {
+        q.state_stride = serve_mp_state_stride(r->words);
+        MDZ_CUDA_TRY(cudaMemcpyAsync(&d->req[r->slot], &q, sizeof q, cudaMemcpyHostToDevice,
+                                     main));
+        int rc = launch_serve_enqueue(d, r->cls, (int)cur, r->slot, (unsigned)r->npix, main);
+        if (rc)
+            return rc;
+        qhost[r->cls] += (long)r->npix;
+        r->phase = kRunning;
+        std::lock_guard<std::mutex> lk(mu);
+        st.launches += 2;
+    }
+    return MDZGPU_OK;
+}
+
+void Server::poll_orbits()
+{
+    for (auto& r : slots) {
+        if (!r || r->phase != kOrbit)
+            continue;
+        const cudaError_t e = cudaEventQuery(r->ev_orbit);
+        if (e == cudaErrorNotReady)
+            continue;
+        if (e != cudaSuccess) {
+            set_error("serve: reference orbit failed: %s", cudaGetErrorString(e));
+            auto keep = r;
+            end(keep, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
+            continue;
+        }
+        bool cancel;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            cancel = r->cancel;
+            st.launches += 2;  // orbit + finish kernels
+        }
+        if (cancel) {
+            auto keep = r;
+            end(keep, keep->cancel_state, 0);
+            continue;
+        }
+        if (launch_serve_enqueue(d, 0, (int)cur, r->slot, (unsigned)r->npix, main)) {
+            auto keep = r;
+            end(keep, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
+            continue;
+        }
+        qhost[0] += (long)r->npix;
+        r->phase = kRunning;
+        std::lock_guard<std::mutex> lk(mu);
+        st.launches += 2;
+    }
+}
+
+int Server::step()
+{
+    // budgets: each running request gets an equal share of the step
+    int R = 0;
+    for (auto& r : slots)
+        R += r && r->phase == kRunning;
+    memset(ctl_h, 0, sizeof(ServeCtl));
+    ctl_h->cur = cur;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (int s = 0; s < kServeSlots; ++s) {
+            const auto& r = slots[s];
+            if (!r || r->phase != kRunning)
+                continue;
+            if (r->cancel)
+                ctl_h->cancel |= 1ull << s;
+            unsigned left = status_h->remaining[s];
+            if (left == 0 || left > r->npix)
+                left = (unsigned)r->npix;  // enqueued since the last status
+            const double b = cfg.step_ms * 1e-3 * class_rate(r->cls) / ((double)R * left);
+            const double bmin = r->cls == 0 ? 256.0 : 16.0;
+            ctl_h->budget[s] = (unsigned)std::min(std::max(b, bmin), (double)(1u << 24));
+        }
+    }
+    const double t0 = wall_ms();
+    MDZ_CUDA_TRY(cudaGraphLaunch(step_exec, main));
+    MDZ_CUDA_TRY(cudaStreamSynchronize(main));
+    const double t1 = wall_ms();
+    cur ^= 1u;
+    for (int c = 0; c < kServeClasses; ++c)
+        qhost[c] = (long)status_h->qcount[c][cur];
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        st.steps++;
+        st.launches += launches_per_step;
+        st.busy_ms += t1 - t0;
+    }
+    for (int s = 0; s < kServeSlots; ++s) {
+        auto r = slots[s];
+        if (!r || r->phase != kRunning)
+            continue;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            r->steps++;
+        }
+        if (status_h->remaining[s] != 0) {
+            if (qhost[r->cls] == 0) {
+                // pixels neither finished nor queued: never expected; fail the
+                // request rather than wait for it forever
+                set_error("serve: request %lld lost %u pixels", (long long)r->id,
+                          status_h->remaining[s]);
+                end(r, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
+            }
+            continue;
+        }
+        bool cancel;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            cancel = r->cancel;
+        }
+        if (cancel) {
+            end(r, r->cancel_state, 0);
+            continue;
+        }
+        const int rc = start_finish(r);
+        if (rc)
+            end(r, MDZGPU_REQ_FAILED, rc);
+    }
+    return MDZGPU_OK;
+}
+
+// Main pass done: escalation passes (perturbation) and the copies out.
+int Server::start_finish(const std::shared_ptr<Req>& r)
+{
+    const Layout& l = r->lay;
+    char* db = arena_dev + r->dev_off;
+    char* hb = stage_host + r->host_off;
+    cudaStream_t s = side[r->slot];
+    int launches = 0;
+    if (r->method == MDZGPU_METHOD_PERTURB) {
+        mdzgpu_ctx shape;  // the list passes read only the SM count
+        shape.device = device;
+        shape.num_sms = num_sms;
+        PerturbLaunch p = req_h[r->slot].pl;
+        unsigned* counts_dev = (unsigned*)(db + l.lists);
+        unsigned* list1 = (unsigned*)(db + l.lists + 256);
+        unsigned* list2 = list1 + r->npix;
+        MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, s));
+        p.list_in = list1;
+        p.list_in_count = counts_dev;
+        p.lost_limit = 6.0f;  // FP64 pass: bits before the multi-limb re-run
+        p.flag_out = list2;
+        p.flag_out_count = counts_dev + 1;
+        int rc = launch_perturb(&shape, p, s, 1);
+        if (rc) {
+            shape.stream = nullptr;
+            return rc;
+        }
+        MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, s));
+        MpLaunch q;
+        q.W = r->W;
+        q.H = r->H;
+        q.row0 = 0;
+        q.nrows = r->H;
+        q.family = MDZ_FAMILY_MANDEL;
+        q.fractal = MDZ_MANDELBROT;
+        q.depth = r->depth;
+        q.words = r->words;
+        q.xs = (const uint32_t*)(db + l.tables);
+        q.ys = q.xs + (size_t)r->W * r->words;
+        q.julia = q.xs;
+        q.out = p.out;
+        q.sync = (FrameSync*)(db + l.sync);
+        q.tile_rows_done = nullptr;
+        q.band_flags = nullptr;
+        q.stop = nullptr;
+        q.list = list2;
+        q.list_count = counts_dev + 1;
+        q.mag = p.mag;
+        rc = launch_mp(&shape, q, s);
+        shape.stream = nullptr;
+        if (rc)
+            return rc;
+        launches += 2;
+        MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_misc, counts_dev, 8, cudaMemcpyDeviceToHost, s));
+        MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_misc + 8, db + l.orbit + l.ol.reb, 8,
+                                     cudaMemcpyDeviceToHost, s));
+    }
+    MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_counts, db + l.counts, r->npix * 4,
+                                 cudaMemcpyDeviceToHost, s));
+    if (r->want_mag)
+        MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_mag, db + l.mag, r->npix * 4,
+                                     cudaMemcpyDeviceToHost, s));
+    MDZ_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_done, cudaEventDisableTiming));
+    MDZ_CUDA_TRY(cudaEventRecord(r->ev_done, s));
+    r->phase = kFinishing;
+    std::lock_guard<std::mutex> lk(mu);
+    st.launches += launches;
+    return MDZGPU_OK;
+}
+
+void Server::poll_finishing()
+{
+    for (auto& slot_ref : slots) {
+        auto r = slot_ref;
+        if (!r || r->phase != kFinishing)
+            continue;
+        const cudaError_t e = cudaEventQuery(r->ev_done);
+        if (e == cudaErrorNotReady)
+            continue;
+        if (e != cudaSuccess) {
+            set_error("serve: request %lld failed: %s", (long long)r->id, cudaGetErrorString(e));
+            end(r, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
+            continue;
+        }
+        const Layout& l = r->lay;
+        const char* hb = stage_host + r->host_off;
+        const int32_t* c = (const int32_t*)(hb + l.h_counts);
+        memcpy(r->out_counts, c, r->npix * 4);
+        if (r->want_mag)
+            memcpy(r->out_mag, hb + l.h_mag, r->npix * 4);
+        int64_t its = 0;
+        for (size_t i = 0; i < r->npix; ++i)
+            its += c[i] ? c[i] : (int64_t)r->depth;
+        r->pixel_iters = its;
+        if (r->method == MDZGPU_METHOD_PERTURB) {
+            const unsigned* esc = (const unsigned*)(hb + l.h_misc);
+            r->esc_fp64 = esc[0];
+            r->esc_mp = esc[1];
+            unsigned long long reb;
+            memcpy(&reb, hb + l.h_misc + 8, 8);
+            r->rebases = (int64_t)reb;
+        }
+        end(r, MDZGPU_REQ_DONE, 0);
+    }
+}
+
+void Server::run()
+{
+    cudaSetDevice(device);
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            if (quit)
+                break;
+            bool idle = waiting.empty();
+            for (const auto& s : slots)
+                idle = idle && !s;
+            if (idle)
+                cv_work.wait_for(lk, std::chrono::milliseconds(20));
+            if (quit)
+                break;
+        }
+        check_cancels();
+        admit();
+        poll_orbits();
+        long queued = 0;
+        for (long q : qhost)
+            queued += q;
+        if (queued > 0) {
+            if (step()) {
+                // a failed step leaves the device state unknown: fail everything
+                for (auto& s : slots)
+                    if (s) {
+                        auto keep = s;
+                        cudaStreamSynchronize(side[keep->slot]);
+                        end(keep, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
+                    }
+                for (long& q : qhost)
+                    q = 0;
+            }
+        }
+        poll_finishing();
+        if (queued == 0) {
+            bool waiting_gpu = false;
+            for (const auto& s : slots)
+                waiting_gpu = waiting_gpu || (s && (s->phase == kOrbit || s->phase == kFinishing));
+            if (waiting_gpu)
+                std::this_thread::sleep_for(std::chrono::microseconds(100));
+        }
+    }
+    // shutdown: let the GPU work in flight end, then cancel what is left
+    cudaStreamSynchronize(main);
+    for (auto& s : side)
+        cudaStreamSynchronize(s);
+    for (auto& s : slots)
+        if (s) {
+            auto keep = s;
+            end(keep, MDZGPU_REQ_CANCELLED, 0);
+        }
+    std::deque<std::shared_ptr<Req>> left;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        left.swap(waiting);
+    }
+    for (auto& r : left)
+        end(r, MDZGPU_REQ_CANCELLED, 0);
+}
+
+void Server::teardown()
+{
+    if (th.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            quit = true;
+        }
+        cv_work.notify_all();
+        th.join();
+    }
+    if (main)
+        cudaStreamSynchronize(main);
+    if (step_exec)
+        cudaGraphExecDestroy(step_exec);
+    if (graph)
+        cudaGraphDestroy(graph);
+    for (auto& e : join)
+        if (e)
+            cudaEventDestroy(e);
+    if (fork)
+        cudaEventDestroy(fork);
+    for (auto& s : branch)
+        if (s)
+            cudaStreamDestroy(s);
+    for (auto& s : side)
+        if (s)
+            cudaStreamDestroy(s);
+    if (main)
+        cudaStreamDestroy(main);
+    cudaFree(arena_dev);
+    cudaFree(queues);
+    cudaFree(d);
+    cudaFreeHost(stage_host);
+    cudaFreeHost(ctl_h);
+    cudaFreeHost(status_h);
+    cudaFreeHost(req_h);
+    if (log)
+        fclose(log);
+}
+
+}  // namespace mdz
+
+using namespace mdz;
+
+struct mdzgpu_server {
+    Server s;
+};
+
+extern "C" {
+
+mdzgpu_server* mdzgpu_serve_create(const mdzgpu_serve_config* cfg)
+{
+    auto* srv = new mdzgpu_server();
+    if (srv->s.init(cfg)) {
+        srv->s.teardown();
+        delete srv;
+        return nullptr;
+    }
+    return srv;
+}
+
+void mdzgpu_serve_destroy(mdzgpu_server* srv)
+{
+    if (!srv)
+        return;
+    srv->s.teardown();
+    delete srv;
+}
+
+int mdzgpu_serve_footprint(const mdzgpu_request* q, int64_t* device_bytes, int64_t* host_bytes)
+{
+    Req r;
+    const int rc = prepare(q, r);
+    if (rc)
+        return rc;
+    if (device_bytes)
+        *device_bytes = (int64_t)r.lay.dev_bytes;
+    if (host_bytes)
+        *host_bytes = (int64_t)r.lay.host_bytes;
+    return MDZGPU_OK;
+}
+
+int mdzgpu_serve_submit(mdzgpu_server* srv, const mdzgpu_request* q, int64_t* id)
+{
+    if (!srv) {
+        set_error("serve: null server");
+        return MDZGPU_ERR_ARG;
+    }
+    Server& s = srv->s;
+    auto r = std::make_shared<Req>();
+    int rc = prepare(q, *r);
+    if (rc) {
+        std::lock_guard<std::mutex> lk(s.mu);
+        s.st.submitted++;
+        s.st.failed++;
+        return rc;
+    }
+    if (r->lay.dev_bytes > s.arena.size() || r->lay.host_bytes > s.stage.size()
+        || (long)r->npix > s.cfg.queue_pixels) {
+        set_error("serve: request needs %zu device / %zu host bytes; the server has %lld / %lld",
+                  r->lay.dev_bytes, r->lay.host_bytes, (long long)s.cfg.arena_bytes,
+                  (long long)s.cfg.staging_bytes);
+        std::lock_guard<std::mutex> lk(s.mu);
+        s.st.submitted++;
+        s.st.failed++;
+        return MDZGPU_ERR_NOMEM;
+    }
+    {
+        std::lock_guard<std::mutex> lk(s.mu);
+        if (s.quit) {
+            set_error("serve: server is stopping");
+            return MDZGPU_ERR_STOPPED;
+        }
+        r->id = s.next_id++;
+        r->t_submit = wall_ms();
+        s.all[r->id] = r;
+        s.waiting.push_back(r);
+        s.st.submitted++;
+    }
+    s.cv_work.notify_all();
+    if (id)
+        *id = r->id;
+    return MDZGPU_OK;
+}
+
+static void fill_status(const Req& r, mdzgpu_request_status* out)
+{
+    memset(out, 0, sizeof *out);
+    out->state = r.state;
+    out->error = r.error;
+    out->method = r.method;
+    out->words = r.method == MDZGPU_METHOD_PERTURB ? r.limbs : r.words;
+    out->queue_ms = r.t_admit > 0 ? r.t_admit - r.t_submit : 0.0;
+    out->latency_ms = r.t_done > 0 ? r.t_done - r.t_submit : 0.0;
+    out->pixel_iters = r.pixel_iters;
+    out->escalated_fp64 = r.esc_fp64;
+    out->escalated_mp = r.esc_mp;
+    out->rebases = r.rebases;
+    out->steps = r.steps;
+}
+
+int mdzgpu_serve_poll(mdzgpu_server* srv, int64_t id, mdzgpu_request_status* out)
+{
+    if (!srv || !out) {
+        set_error("serve: null argument");
+        return MDZGPU_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(srv->s.mu);
+    auto it = srv->s.all.find(id);
+    if (it == srv->s.all.end()) {
+        set_error("serve: unknown request %lld", (long long)id);
+        return MDZGPU_ERR_ARG;
+    }
+    fill_status(*it->second, out);
+    return MDZGPU_OK;
+}
+
+int mdzgpu_serve_wait(mdzgpu_server* srv, int64_t id, double timeout_ms,
+                      mdzgpu_request_status* out)
+{
+    if (!srv) {
+        set_error("serve: null server");
+        return MDZGPU_ERR_ARG;
+    }
+    Server& s = srv->s;
+    std::unique_lock<std::mutex> lk(s.mu);
+    auto it = s.all.find(id);
+    if (it == s.all.end()) {
+        set_error("serve: unknown request %lld", (long long)id);
+        return MDZGPU_ERR_ARG;
+    }
+    auto r = it->second;
+    auto finished = [&] {
+        return r->state != MDZGPU_REQ_QUEUED && r->state != MDZGPU_REQ_RUNNING;
+    };
+    if (timeout_ms < 0)
+        s.cv_done.wait(lk, finished);
+    else
+        s.cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), finished);
+    if (out)
+        fill_status(*r, out);
+    if (!finished()) {
+        set_error("serve: request %lld still running", (long long)id);
+        return MDZGPU_ERR_TIMEOUT;
+    }
+    return MDZGPU_OK;
+}
+
+int mdzgpu_serve_cancel(mdzgpu_server* srv, int64_t id)
+{
+    if (!srv) {
+        set_error("serve: null server");
+        return MDZGPU_ERR_ARG;
+    }
+    {
+        std::lock_guard<std::mutex> lk(srv->s.mu);
+        auto it = srv->s.all.find(id);
+        if (it == srv->s.all.end()) {
+            set_error("serve: unknown request %lld", (long long)id);
+            return MDZGPU_ERR_ARG;
+        }
+        it->second->cancel = true;
+        it->second->cancel_state = MDZGPU_REQ_CANCELLED;
+    }
+    srv->s.cv_work.notify_all();
+    return MDZGPU_OK;
+}
+
+int mdzgpu_serve_release(mdzgpu_server* srv, int64_t id)
+{
+    if (!srv) {
+        set_error("serve: null server");
+        return MDZGPU_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(srv->s.mu);
+    auto it = srv->s.all.find(id);
+    if (it == srv->s.all.end()) {
+        set_error("serve: unknown request %lld", (long long)id);
+        return MDZGPU_ERR_ARG;
+    }
+    const int state = it->second->state;
+    if (state == MDZGPU_REQ_QUEUED || state == MDZGPU_REQ_RUNNING) {
+        set_error("serve: request %lld has not finished", (long long)id);
+        return MDZGPU_ERR_ARG;
+    }
+    srv->s.all.erase(it);
+    return MDZGPU_OK;
+}
+
+int mdzgpu_serve_get_stats(mdzgpu_server* srv, mdzgpu_serve_stats* out)
+{
+    if (!srv || !out) {
+        set_error("serve: null argument");
+        return MDZGPU_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(srv->s.mu);
+    *out = srv->s.st;
+    std::vector<double> v = srv->s.latencies;
+    if (!v.empty()) {
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double q) {
+            // nearest-rank percentile
+            size_t k = (size_t)ceil(q * (double)v.size());
+            if (k < 1)
+                k = 1;
+            return v[std::min(k, v.size()) - 1];
+        };
+        out->latency_p50_ms = pct(0.50);
+        out->latency_p99_ms = pct(0.99);
+        out->latency_max_ms = v.back();
+    }
+    return MDZGPU_OK;
+}
+
+}  // extern "C"

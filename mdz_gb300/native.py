@@ -39,6 +39,43 @@ class MpValStruct(C.Structure):
                 ("d", C.POINTER(C.c_uint64))]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_requests", C.c_int32),
+                ("arena_bytes", C.c_int64), ("staging_bytes", C.c_int64),
+                ("queue_pixels", C.c_int64), ("step_ms", C.c_double),
+                ("log_path", C.c_char_p)]
+
+
+class Request(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("family", C.c_int32),
+                ("fractal", C.c_int32), ("depth", C.c_int64), ("precision", C.c_int64),
+                ("cx", MpValStruct), ("cy", MpValStruct), ("span", MpValStruct),
+                ("method", C.c_int32), ("pad", C.c_int32), ("timeout_ms", C.c_double),
+                ("counts", C.c_void_p), ("mag2", C.c_void_p)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("error", C.c_int32), ("method", C.c_int32),
+                ("words", C.c_int32), ("queue_ms", C.c_double), ("latency_ms", C.c_double),
+                ("pixel_iters", C.c_int64), ("escalated_fp64", C.c_int64),
+                ("escalated_mp", C.c_int64), ("rebases", C.c_int64), ("steps", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("cancelled", C.c_int64), ("timed_out", C.c_int64), ("steps", C.c_int64),
+                ("launches", C.c_int64), ("pixel_iters", C.c_int64), ("busy_ms", C.c_double),
+                ("latency_p50_ms", C.c_double), ("latency_p99_ms", C.c_double),
+                ("latency_max_ms", C.c_double), ("device_bytes_in_use", C.c_int64),
+                ("device_bytes_peak", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 P = C.c_void_p
 _SIGS = {
     "mdzgpu_create": (P, [C.c_int]),
@@ -73,6 +110,17 @@ _SIGS = {
                               + [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int32, P, P]),
     "mdzgpu_abi_layout": (C.c_int, [P, C.c_int]),
     "mdzgpu_measure_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    # serving engine
+    "mdzgpu_serve_create": (P, [C.POINTER(ServeConfig)]),
+    "mdzgpu_serve_destroy": (None, [P]),
+    "mdzgpu_serve_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_int64)]),
+    "mdzgpu_serve_poll": (C.c_int, [P, C.c_int64, C.POINTER(RequestStatus)]),
+    "mdzgpu_serve_wait": (C.c_int, [P, C.c_int64, C.c_double, C.POINTER(RequestStatus)]),
+    "mdzgpu_serve_cancel": (C.c_int, [P, C.c_int64]),
+    "mdzgpu_serve_release": (C.c_int, [P, C.c_int64]),
+    "mdzgpu_serve_get_stats": (C.c_int, [P, C.POINTER(ServeStats)]),
+    "mdzgpu_serve_footprint": (C.c_int, [C.POINTER(Request), C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int64)]),
     # drop-in layer
     "rth_create": (P, []),
     "rth_init": (C.c_int, [P, C.c_int, C.c_int, P]),

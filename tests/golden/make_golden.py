@@ -6,6 +6,7 @@ the reference sources exist; the GPU machine only reads the outputs).
   python tests/golden/make_golden.py mp        # mp_*.npz    (reference MPFR path, p and 2p)
   python tests/golden/make_golden.py perturb   # perturb_c4.npz (MPFR at 2176 bits)
   python tests/golden/make_golden.py abi       # abi_layout.json (reference struct offsets)
+  python tests/golden/make_golden.py centres   # serve_centres.json (serving stream centres)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -100,7 +101,7 @@ def ray_dir(seed: int) -> tuple[float, float]:
     return math.cos(theta), math.sin(theta)
 
 
-def bisect_fp64(seed: int, depth: int) -> tuple[float, float]:
+def bisect_fp64(seed: int, depth: int, fractal: int = 0) -> tuple[float, float]:
     """Ray from 0 at a seeded angle; bisect r in [0, 2] on 'count == 0 at
     depth' (reference double loop) to 53-bit precision."""
     ct, st = ray_dir(seed)
@@ -109,14 +110,15 @@ def bisect_fp64(seed: int, depth: int) -> tuple[float, float]:
         mid = 0.5 * (lo + hi)
         if mid == lo or mid == hi:
             break
-        if O.lib().mdzo_point_fp64(0, depth, mid * ct, mid * st) == 0:
+        if O.lib().mdzo_point_fp64(fractal, depth, mid * ct, mid * st) == 0:
             lo = mid
         else:
             hi = mid
     return lo * ct, lo * st
 
 
-def bisect_mpfr(seed: int, depth: int, prec: int, start_bits: int = 50) -> tuple[Fraction, Fraction]:
+def bisect_mpfr(seed: int, depth: int, prec: int, start_bits: int = 50,
+                fractal: int = 0) -> tuple[Fraction, Fraction]:
     """The same ray bisection continued in MPFR at `prec` bits; 7 points per
     round on THREADS cores (an 8-ary search, 3 bits per round)."""
     ct, st = (Fraction(x) for x in ray_dir(seed))
@@ -124,7 +126,7 @@ def bisect_mpfr(seed: int, depth: int, prec: int, start_bits: int = 50) -> tuple
     # coarse stage in FP64 (identical predicate where doubles suffice)
     for _ in range(start_bits):
         mid = (lo + hi) / 2
-        if O.lib().mdzo_point_fp64(0, depth, float(mid * ct), float(mid * st)) == 0:
+        if O.lib().mdzo_point_fp64(fractal, depth, float(mid * ct), float(mid * st)) == 0:
             lo = mid
         else:
             hi = mid
@@ -133,7 +135,7 @@ def bisect_mpfr(seed: int, depth: int, prec: int, start_bits: int = 50) -> tuple
         pts = [lo + (hi - lo) * i / k for i in range(1, k)]
         cre = [MpVal.from_fraction(p * ct, prec).hex() for p in pts]
         cim = [MpVal.from_fraction(p * st, prec).hex() for p in pts]
-        counts, _ = O.points_mpfr(cre, cim, depth, prec, threads=THREADS)
+        counts, _ = O.points_mpfr(cre, cim, depth, prec, fractal=fractal, threads=THREADS)
         inside = [c == 0 for c in counts]
         # last inside point before the first outside one
         new_lo, new_hi = lo, hi
@@ -181,6 +183,28 @@ def make_views() -> None:
                        aa=1, seed=4)
     print("c4", f"{time.time() - t0:.1f}s")
     (GOLD / "views.json").write_text(json.dumps(views, indent=1))
+
+
+# Centre pool of the serving stream: seeded ray bisection per formula,
+# refined to 1100 bits (enough for every precision of the stream,
+# ceil(-log2 width) + 64 <= 1064).  The stream draws each request's centre
+# from this pool.
+SERVE_POOL = {0: range(5000, 5012), 1: range(6000, 6006), 2: range(7000, 7006)}
+SERVE_BISECT_DEPTH = 10000
+SERVE_PREC = 1100
+
+
+def make_centres() -> None:
+    out = {"bisect_depth": SERVE_BISECT_DEPTH, "prec": SERVE_PREC, "centres": []}
+    for fractal, seeds in SERVE_POOL.items():
+        for seed in seeds:
+            t0 = time.time()
+            bre, bim = bisect_mpfr(seed=seed, depth=SERVE_BISECT_DEPTH, prec=SERVE_PREC,
+                                   fractal=fractal)
+            out["centres"].append(dict(fractal=fractal, seed=seed, cx=hexfloat(bre),
+                                       cy=hexfloat(bim)))
+            print("centre", fractal, seed, f"{time.time() - t0:.1f}s", flush=True)
+            (GOLD / "serve_centres.json").write_text(json.dumps(out, indent=1))
 
 
 # --------------------------------------------------------------------------
@@ -438,7 +462,7 @@ def main(argv: list[str]) -> None:
     what = argv[1:] or ["fp64"]
     for w in what:
         {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
-         "perturb": make_perturb}[w]()
+         "perturb": make_perturb, "centres": make_centres}[w]()
 
 
 if __name__ == "__main__":
