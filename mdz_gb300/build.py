@@ -60,6 +60,7 @@ def _newest_header() -> float:
 
 def _compile(job, verbose: bool) -> str:
     src, obj, extra = job
+    extra = extra + os.environ.get("MDZGPU_NVCC_FLAGS", "").split()
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
         cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-x", "cu", *extra, "-I", str(INCLUDE), "-c", str(src),

@@ -1,0 +1,79 @@
+"""One render of each GPU path on the seeded views, for profiling and timing.
+
+    python -m mdz_gb300.cases c2 [--frame 480x270] [--repeat 1]
+    python -m mdz_gb300.cases c3 | c4 | serve [--requests 4]
+
+c1/c2: FP64 kernel (MDZ's double path) on the views' rectangles (c2 without
+supersampling unless --aa); c3: the multi-limb kernel at 256 bits; c4: the
+perturbation frame (orbit + FP32 pixels + escalation passes); serve: the
+first requests of the seeded serving stream through the serving engine.
+--frame keeps the view's pixel spacing and crops around its centre.
+Prints one JSON line of the call's statistics per repeat.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+from fractions import Fraction
+from pathlib import Path
+
+from . import MpVal, Renderer, View, parse_number
+
+VIEWS = json.loads((Path(__file__).resolve().parents[1] / "tests" / "golden" /
+                    "views.json").read_text())
+
+
+def view(name: str, frame: str | None, aa: bool) -> View:
+    d = dict(VIEWS[name])
+    if not aa:
+        d["aa"] = 1
+    if frame:
+        w, h = (int(x) for x in frame.lower().split("x"))
+        d["size"] = str(parse_number(d["size"]) * Fraction(w, d["width"]))
+        d["width"], d["height"] = w, h
+    return View.from_dict(d)
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["c1", "c2", "c3", "c4", "serve"])
+    ap.add_argument("--frame", default=None)
+    ap.add_argument("--aa", action="store_true")
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--requests", type=int, default=4)
+    a = ap.parse_args(argv)
+    if a.case == "serve":
+        from .serve import Server
+        from .stream import load_pool, make_stream
+        pool = load_pool()
+        items = make_stream(a.requests, pool)
+        with Server(0, arena_bytes=16 << 30) as srv:
+            for _ in range(a.repeat):
+                ids = [srv.submit(it.request(pool)) for it in items]
+                sts = [srv.wait(i) for i in ids]
+                print(json.dumps({"requests": len(sts), "states": [s["state"] for s in sts],
+                                  "stats": srv.stats()}), flush=True)
+        return
+    v = view(a.case, a.frame, a.aa)
+    with Renderer(0) as r:
+        for _ in range(a.repeat):
+            if a.case in ("c1", "c2"):
+                xmin, xmax, ymax = v.rect().doubles()
+                _, st = r.render_fp64(v.real_width, v.real_height, v.depth, xmin, xmax, ymax)
+            elif a.case == "c3":
+                rc = v.rect()
+                _, st = r.render_mp(v.real_width, v.real_height, v.depth, rc.xmin, rc.ymax,
+                                    rc.width, v.precision)
+            else:
+                prec = v.precision
+                cx = MpVal.from_fraction(parse_number(v.cx), prec)
+                cy = MpVal.from_fraction(parse_number(v.cy), prec)
+                w = MpVal.from_fraction(parse_number(v.size), prec)
+                _, _, st = r.render_perturb(v.real_width, v.real_height, v.depth, cx, cy, w,
+                                            prec)
+            print(json.dumps(st), flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -5,6 +5,7 @@
 #include <stddef.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <string>
 #include <vector>
@@ -206,8 +207,12 @@ mdzgpu_ctx* mdzgpu_create(int device)
     auto* ctx = new mdzgpu_ctx();
     ctx->device = device;
     ctx->num_sms = prop.multiProcessorCount;
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess
-        || cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        || cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess
+        || cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess
+        || cudaEventCreate(&ctx->ev_side0) != cudaSuccess) {
         set_error("stream/event creation failed");
         delete ctx;
         return nullptr;
@@ -230,8 +235,14 @@ void mdzgpu_destroy(mdzgpu_ctx* ctx)
     ctx->lists.release();
     ctx->pinned.release();
     ctx->staging.release();
+    ctx->pstate.release();
+    ctx->pqueue.release();
+    ctx->stepinfo.release();
+    cudaStreamSynchronize(ctx->side);
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
+    cudaEventDestroy(ctx->ev_side0);
+    cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -603,6 +614,64 @@ int perturb_tables(const mdzgpu_mpval* cx, const mdzgpu_mpval* cy, double hs_m, 
 
 extern "C" {
 
+// Pass 0 in steps while the streamed orbit (already launched on ctx->side,
+// completion event `orbit_done_ev`) is produced.  Each step: every
+// unfinished pixel runs at most `budget` iterations or up to the last
+// finished orbit entry; the unfinished ones are compacted into the other
+// queue.  The budget keeps one step near 8 ms of GPU time.
+static int perturb_steps(mdzgpu_ctx* ctx, const PerturbLaunch& p, size_t n,
+                         cudaEvent_t orbit_done_ev, int* launches)
+{
+    int rc;
+    if ((rc = ctx->pstate.ensure(n * 32)) || (rc = ctx->pqueue.ensure(2 * n * 4 + 256))
+        || (rc = ctx->stepinfo.ensure(256)))
+        return rc;
+    unsigned* counters = (unsigned*)ctx->pqueue.ptr;           // pull, count
+    unsigned* qa = (unsigned*)((char*)ctx->pqueue.ptr + 256);
+    unsigned* qb = qa + n;
+    volatile unsigned* h_count = (volatile unsigned*)ctx->stepinfo.host;
+    volatile int* h_orbit_err = (volatile int*)ctx->stepinfo.host + 1;
+    const unsigned* in = nullptr;   // first step: every pixel, fresh
+    unsigned* out = qa;
+    unsigned left = (unsigned)n;
+    bool orbit_finished = false;
+    // a pixel stops at least every `budget` iterations, or when it waits for
+    // the orbit: after the orbit is complete every step advances every
+    // pixel, so the loop ends within depth / budget_min steps of it
+    const double rate = 3.0e11;       // pixel-iterations/s of the FP32 pass
+    for (long step = 0;; ++step) {
+        const double b = rate * 8e-3 / (double)left;
+        const unsigned budget = (unsigned)std::min(std::max(b, 256.0), (double)(1u << 24));
+        if ((rc = launch_perturb_step(ctx->num_sms, p, in, left, out, counters,
+                                      (uint4*)ctx->pstate.ptr, budget, ctx->stream)))
+            return rc;
+        MDZ_CUDA_TRY(cudaMemcpyAsync((void*)h_count, counters + 1, 4, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        MDZ_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        *launches += 2;
+        left = *h_count;
+        if (left == 0)
+            return MDZGPU_OK;
+        in = out;
+        out = (out == qa) ? qb : qa;
+        if (!orbit_finished) {
+            const cudaError_t e = cudaEventQuery(orbit_done_ev);
+            if (e == cudaSuccess) {
+                orbit_finished = true;
+                MDZ_CUDA_TRY(cudaMemcpyAsync((void*)h_orbit_err, p.orbit_error, 4,
+                                             cudaMemcpyDeviceToHost, ctx->side));
+                MDZ_CUDA_TRY(cudaStreamSynchronize(ctx->side));
+                if (*h_orbit_err) {
+                    set_error("perturbation: a bounded wait of the orbit finisher gave up");
+                    return MDZGPU_ERR_TIMEOUT;
+                }
+            } else if (e != cudaErrorNotReady) {
+                MDZ_CUDA_TRY(e);
+            }
+        }
+    }
+}
+
 static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,
                           const mdzgpu_mpval* cy, const mdzgpu_mpval* width, int64_t precision,
                           int32_t limbs, int32_t* d_out, float* d_mag, int32_t* h_out,
@@ -681,20 +750,39 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     // progress words of the fused launch live beside out_len
     int* prog = (int*)(ob + off_len);
     MDZ_CUDA_TRY(cudaMemsetAsync(prog, 0, 256, ctx->stream));
-    // MDZGPU_FUSED=1: orbit and FP32 pixel pass in one cooperative launch.
-    // Off by default: a persistent grid holds a fraction of the frame's tiles,
-    // so the first wave is paced by the serial orbit (measured slower than
-    // the separate launches); the serving engine overlaps orbits instead.
+    // Pass 0 schedule (MDZGPU_PERTURB):
+    //   "steps" (default): the orbit runs as a cooperative producer/finisher
+    //     launch on the side stream while the frame's pixels iterate in
+    //     steps on the main stream; a step lets every unfinished pixel run
+    //     until its budget or the last finished orbit entry, then compacts
+    //     the unfinished pixels; the orbit's serial time hides behind the
+    //     pixel work;
+    //   "frame": the orbit first, then one launch over the whole frame;
+    //   "fused": orbit and pixels in one cooperative grid (slower: the
+    //     resident first wave is paced by the orbit).
+    const char* menv = getenv("MDZGPU_PERTURB");
     const char* fenv = getenv("MDZGPU_FUSED");
-    const bool fused = fenv && fenv[0] == '1';
+    const bool fused = (fenv && fenv[0] == '1') || (menv && !strcmp(menv, "fused"));
+    const bool stepped = !fused && !(menv && !strcmp(menv, "frame"));
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
-    if (!fused) {
-        if ((rc = launch_orbit(o, ctx->stream))) {
+    if (stepped) {
+        MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->stream));   // inputs in place
+        MDZ_CUDA_TRY(cudaStreamWaitEvent(ctx->side, evo, 0));
+        MDZ_CUDA_TRY(cudaEventRecord(ctx->ev_side0, ctx->side));
+        if ((rc = launch_orbit_stream(o, prog, ctx->side))) {
             cudaEventDestroy(evo);
             return rc;
         }
+        MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->side));      // orbit complete
+    } else {
+        if (!fused) {
+            if ((rc = launch_orbit(o, ctx->stream))) {
+                cudaEventDestroy(evo);
+                return rc;
+            }
+        }
+        MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->stream));
     }
-    MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->stream));
     PerturbLaunch p;
     p.W = f->width;
     p.H = f->height;
@@ -733,7 +821,15 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.orbit_done = prog + 3;
     p.orbit_error = prog + 4;
     p.producer_sm = prog + 5;
-    rc = fused ? launch_fused(ctx, o, p, ctx->stream) : launch_perturb(ctx, p, ctx->stream, 0);
+    int launches = 5;
+    if (stepped) {
+        rc = perturb_steps(ctx, p, n, evo, &launches);
+        // the list passes read the whole orbit
+        if (!rc && cudaStreamWaitEvent(ctx->stream, evo, 0) != cudaSuccess)
+            rc = MDZGPU_ERR_CUDA;
+    } else {
+        rc = fused ? launch_fused(ctx, o, p, ctx->stream) : launch_perturb(ctx, p, ctx->stream, 0);
+    }
     if (rc) {
         cudaEventDestroy(evo);
         return rc;
@@ -810,7 +906,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     MDZ_CUDA_TRY(cudaMemcpyAsync(esc, counts_dev, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(&reb, p.rebases, 8, cudaMemcpyDeviceToHost, ctx->stream));
     MDZ_CUDA_TRY(cudaMemcpyAsync(&olen, o.out_len, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    rc = finish_stats(ctx, st, t0, 5, (int64_t)dig.size() * 4 + h2d_extra, d2h + 20);
+    rc = finish_stats(ctx, st, t0, launches, (int64_t)dig.size() * 4 + h2d_extra, d2h + 20);
     if (!rc && orbit_err) {
         set_error("perturbation: a bounded wait on the reference orbit gave up");
         rc = MDZGPU_ERR_TIMEOUT;
@@ -819,7 +915,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         st->escalated_fp64 = esc[0];
         st->escalated_mp = esc[1];
         float oms = 0.f;
-        cudaEventElapsedTime(&oms, ctx->ev0, evo);
+        cudaEventElapsedTime(&oms, stepped ? ctx->ev_side0 : ctx->ev0, evo);
         // fused: the orbit runs inside the pixel kernel and has no own time
         st->orbit_ms = fused ? -1.0 : oms;
         st->rebases = (int64_t)reb;

@@ -57,7 +57,8 @@ struct mdzgpu_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t side = nullptr;   // high priority: the streamed orbit
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_side0 = nullptr;
     mdz::DevBuf counts;     // int32 counts
     mdz::DevBuf sync;       // FrameSync + tile-row counters
     mdz::DevBuf coords;     // fixed-point pixel coordinates (MP path)
@@ -67,6 +68,9 @@ struct mdzgpu_ctx {
     mdz::DevBuf lists;      // escalation pixel lists (perturbation)
     mdz::PinnedBuf pinned;  // small host-mapped status words
     mdz::PinnedBuf staging; // pinned host copy of counts
+    mdz::DevBuf pstate;     // perturbation pixel state between steps (32 B/pixel)
+    mdz::DevBuf pqueue;     // step counters + two pixel queues
+    mdz::PinnedBuf stepinfo;  // step results read by the host
 };
 
 namespace mdz {
@@ -162,6 +166,20 @@ struct PerturbLaunch {
 };
 // pass 0: FP32 frame pass; pass 1: FP64 pass over list_in
 int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass);
+// The orbit as a cooperative producer + finisher launch that publishes its
+// progress: progress[1] digits written, [2] entries finished (in whole
+// batches of 256), [3] producer done (final length in *o.out_len), [4] a
+// bounded wait gave up, [5] SM id + 1 of the producer while it runs.
+int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s);
+// One step of the FP32 pass over the queue in[0..n) (in == nullptr: every
+// pixel of the frame, fresh): pixels read the orbit progress in p (fin_len,
+// orbit_done, orbit_len), iterate at most `budget` iterations, and the
+// unfinished ones go to out; counters[0] = pull counter, counters[1] = out
+// count, counters[2] = working blocks (all reset by the launch).  Blocks
+// placed on the orbit producer's SM (p.producer_sm) leave it to the producer.
+int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in, unsigned n,
+                        unsigned* out, unsigned* counters, uint4* state, unsigned budget,
+                        cudaStream_t s);
 // Orbit + FP32 pixel pass in one cooperative launch (progress words in p).
 int launch_fused(mdzgpu_ctx* ctx, const OrbitLaunch& o, const PerturbLaunch& p, cudaStream_t s);
 

@@ -607,56 +607,170 @@ __device__ __forceinline__ void pixel_start(PixRun<T>& r, double dcm_r, double d
     r.mag = 0.f;
 }
 
+// The hot step t' = 2 Z_m t + s t^2 + dc 2^-e.  Variant 2 (the default)
+// keeps the two products apart: s t^2 is added to dc first, then each
+// 2 Z_m t term enters through an FMA with its exact product (11 FP32 ops).
+// Variants 0 / 1 factor it as t (2 Z_m + s t) (6 / 8 ops) and round
+// w = 2 Z_m + s t before the product; on the gallery views that extra
+// rounding moved 3 of 1728 pixels off the 2x-precision MPFR counts (variant
+// 2: 1), so the factored forms stay opt-in (-DMDZ_STEP_VARIANT=0/1).
+#ifndef MDZ_STEP_VARIANT
+#define MDZ_STEP_VARIANT 2
+#endif
+template <class T>
+__device__ __forceinline__ void fast_step(PixState<T>& st, T Zx, T Zy, T zr, T zi)
+{
+    const T tr = st.tr, ti = st.ti;
+#if MDZ_STEP_VARIANT == 0
+    const T wr = zr + Zx, wi = zi + Zy;
+    st.tr = Mant<T>::fma_(tr, wr, Mant<T>::fma_(-ti, wi, st.dcr));
+    st.ti = Mant<T>::fma_(tr, wi, Mant<T>::fma_(ti, wr, st.dci));
+#elif MDZ_STEP_VARIANT == 1
+    const T wr = Mant<T>::fma_(Zx, (T)2, st.s * tr), wi = Mant<T>::fma_(Zy, (T)2, st.s * ti);
+    st.tr = Mant<T>::fma_(tr, wr, Mant<T>::fma_(-ti, wi, st.dcr));
+    st.ti = Mant<T>::fma_(tr, wi, Mant<T>::fma_(ti, wr, st.dci));
+#else
+    const T u = tr + tr, v = ti + ti;
+    const T a = Mant<T>::fma_(tr, tr, -ti * ti);
+    const T b = tr * v;
+    st.tr = Mant<T>::fma_(Zx, u, Mant<T>::fma_(-Zy, v, Mant<T>::fma_(st.s, a, st.dcr)));
+    st.ti = Mant<T>::fma_(Zx, v, Mant<T>::fma_(Zy, u, Mant<T>::fma_(st.s, b, st.dci)));
+#endif
+}
+
+// How a pixel learns which reference-orbit entries it may read:
+//   kOrbitComplete  the orbit is finished: K = *orbit_len entries;
+//   kOrbitWait      fused launch: wait (bounded) for the finisher;
+//   kOrbitSnapshot  entries below snap.avail are finished (K = snap.K, or
+//                   INT_MAX while the producer runs); a pixel that needs a
+//                   later entry stops and is resumed in a later step.
+enum { kOrbitComplete = 0, kOrbitWait = 1, kOrbitSnapshot = 2 };
+
+struct OrbitSnap {
+    int avail;
+    int K;
+};
+
+// Orbit progress as a step sees it (read once per pixel visit).
+__device__ __forceinline__ OrbitSnap orbit_snapshot(const PerturbLaunch& p)
+{
+    OrbitSnap s;
+    const int done = *(volatile const int*)p.orbit_done;
+    s.K = done ? *(volatile const int*)p.orbit_len : 0x7fffffff;
+    s.avail = *(volatile const int*)p.fin_len;
+    return s;
+}
+
 // Iterations r.wz .. wz_last (inclusive, <= depth).  Returns 1 when the
 // pixel is finished (*count = escape iteration, or 0 at depth), 0 when it
-// stopped after wz_last (state in r), -1 when an orbit wait gave up.
-template <class T, bool STREAM>
+// stopped after wz_last or (snapshot mode) at the last finished orbit entry
+// (state in r), -1 when an orbit wait gave up.
+//
+// One iteration (dz = t 2^e, s = 2^e, z = Z_m + dz):
+//   w  = z + Z_m                        (= 2 Z_m + s t; z carried from the
+//                                         previous iteration's escape test)
+//   t' = t w + dc 2^-e                  (4 FMA: the complex product)
+//   m += 1;  z' = Z_m + s t'  (2 FMA),  |z'|^2 (2)
+//   attention when |z'|^2 > 4 - 2^-14 (escape band) or |z'| <= 2 |dz'|
+//   (the rebase screen; the exact FP64 test decides) or |z'| tiny.
+// Iterations 4k+1 .. 4k+4 whose orbit entries are all finished run as one
+// unrolled block without the orbit, budget and rescale checks; the block
+// leaves at the first iteration that needs attention and that iteration
+// continues on the general path, so the operations are the same whether a
+// pixel runs in blocks or not, and a pixel resumed at any iteration gets
+// bit-identical results.
+template <class T, int MODE>
 __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, double dcm_i,
-                           int dce, uint32_t wz_last, uint32_t& count, BlockOrbitView* view)
+                           int dce, uint32_t wz_last, uint32_t& count, BlockOrbitView* view,
+                           OrbitSnap snap = OrbitSnap{0, 0})
 {
     const T dcf_r = (T)dcm_r, dcf_i = (T)dcm_i;
     PixState<T>& st = r.st;
     int m = r.m;
     // entries 0..avail-1 readable; K = orbit length (unknown while streaming)
-    int K = STREAM ? 0x7fffffff : *p.orbit_len;
-    int avail = K;
-    if (STREAM && !wait_orbit(p, view, m, avail, K))
+    int K = MODE == kOrbitComplete ? *p.orbit_len : (MODE == kOrbitSnapshot ? snap.K : 0x7fffffff);
+    int avail = MODE == kOrbitSnapshot ? snap.avail : K;
+    if (MODE == kOrbitWait && !wait_orbit(p, view, m, avail, K))
         return -1;
+    if (MODE == kOrbitSnapshot && m >= avail)
+        return 0;  // Z_m not finished yet
     T Zx, Zy;
     load_z<T>(p, m, Zx, Zy);
+    T zr = Mant<T>::fma_(st.s, st.tr, Zx);
+    T zi = Mant<T>::fma_(st.s, st.ti, Zy);
     const T band_lo = (T)4 - (T)6.1035156e-5;  // 4 - 2^-14
     const T band_hi = (T)4 + (T)6.1035156e-5;
     T magT = (T)r.mag;
     const uint32_t last = wz_last < p.depth ? wz_last : p.depth;
     uint32_t wz = r.wz;
-    for (; wz <= last; ++wz) {
-        if (m + 1 >= avail) {
-            if (STREAM && m + 1 < K && !wait_orbit(p, view, m + 1, avail, K))
-                return -1;
-            if (m >= K - 1) {
-                // end of the reference orbit: rebase onto Z_0 = 0
-                rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, r.lost, false);
-                m = 0;
-                Zx = (T)0;
-                Zy = (T)0;
-                ++r.rebases;
+    bool blocked = false;
+    while (wz <= last) {
+        bool attention = false;
+        if ((wz & 3u) == 1u && wz + 3u <= last && m + 4 < avail && !st.careful) {
+            // iterations wz .. wz+3, orbit entries m+1 .. m+4 all finished
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                fast_step<T>(st, Zx, Zy, zr, zi);
+                ++m;
+                load_z<T>(p, m, Zx, Zy);
+                zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                magT = Mant<T>::fma_(zr, zr, zi * zi);
+                const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
+                if (magT > band_lo || Mant<T>::fma_(st.s2x4, dd, -magT) >= (T)0
+                    || magT < (T)Mant<T>::kGlitchZ2) {
+                    attention = true;
+                    break;
+                }
+                ++wz;
             }
-        }
-        if (st.careful && (st.force_slow || Zx * Zx + Zy * Zy < (T)Mant<T>::kTinyZ2)) {
-            slow_step<T>(p, m, st, dcf_r, dcf_i, dcm_r, dcm_i, dce);
+            if (!attention) {
+                // wz - 1 = 4k + 4: the rescale check of the general path
+                const T amax = fmax(fabs(st.tr), fabs(st.ti));
+                if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
+                    const int k = Mant<T>::exponent_of(amax);
+                    const T sc = Mant<T>::scale((T)1, -k);
+                    st.tr *= sc;
+                    st.ti *= sc;
+                    st.e += k;
+                    refresh_scale(st, dcf_r, dcf_i, dce);
+                    // as a resumed pixel computes it
+                    zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                    zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                }
+                continue;
+            }
+            // iteration wz is stepped; it continues below
         } else {
-            const T tr = st.tr, ti = st.ti;
-            const T u = tr + tr, v = ti + ti;
-            const T a = Mant<T>::fma_(tr, tr, -ti * ti);  // t^2 real
-            const T b = tr * v;                           // t^2 imag
-            st.tr = Mant<T>::fma_(Zx, u, Mant<T>::fma_(-Zy, v, Mant<T>::fma_(st.s, a, st.dcr)));
-            st.ti = Mant<T>::fma_(Zx, v, Mant<T>::fma_(Zy, u, Mant<T>::fma_(st.s, b, st.dci)));
+            if (m + 1 >= avail) {
+                if (MODE == kOrbitWait && m + 1 < K && !wait_orbit(p, view, m + 1, avail, K))
+                    return -1;
+                if (MODE == kOrbitSnapshot && m + 1 < K) {
+                    blocked = true;  // Z_{m+1} not finished: resume in a later step
+                    break;
+                }
+                if (m >= K - 1) {
+                    // end of the reference orbit: rebase onto Z_0 = 0
+                    rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, r.lost, false);
+                    m = 0;
+                    Zx = (T)0;
+                    Zy = (T)0;
+                    zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                    zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                    ++r.rebases;
+                }
+            }
+            if (st.careful && (st.force_slow || Zx * Zx + Zy * Zy < (T)Mant<T>::kTinyZ2)) {
+                slow_step<T>(p, m, st, dcf_r, dcf_i, dcm_r, dcm_i, dce);
+            } else {
+                fast_step<T>(st, Zx, Zy, zr, zi);
+            }
+            ++m;
+            load_z<T>(p, m, Zx, Zy);
+            zr = Mant<T>::fma_(st.s, st.tr, Zx);
+            zi = Mant<T>::fma_(st.s, st.ti, Zy);
+            magT = Mant<T>::fma_(zr, zr, zi * zi);
         }
-        ++m;
-        load_z<T>(p, m, Zx, Zy);
-        const T zr = Mant<T>::fma_(st.s, st.tr, Zx);
-        const T zi = Mant<T>::fma_(st.s, st.ti, Zy);
-        magT = Mant<T>::fma_(zr, zr, zi * zi);
         if (magT > band_lo) {
             // within 2^-14 of the bailout the rounded Z_m can not decide it
             if (magT > band_hi || escape_exact<T>(p, m, st)) {
@@ -665,16 +779,18 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 return 1;
             }
         }
-        // rebase test |Z_m + dz| < |dz|: it can only hold when
-        // |dz| >= |Z_m| / 2 (or |Z_m| is tiny), checked exactly in FP64
+        // rebase when |Z_m + dz| < |dz|: screened in T as |z| <= 2 |dz| (or
+        // |z| tiny), decided exactly in FP64
         const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
-        const T zn2 = Mant<T>::fma_(Zx, Zx, Zy * Zy);
-        if (Mant<T>::fma_(st.s2x4, dd, -zn2) >= (T)0 || zn2 < (T)Mant<T>::kGlitchZ2) {
+        if (Mant<T>::fma_(st.s2x4, dd, -magT) >= (T)0 || magT < (T)Mant<T>::kGlitchZ2) {
             if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, r.lost, true)) {
                 m = 0;
                 Zx = (T)0;
                 Zy = (T)0;
+                zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                zi = Mant<T>::fma_(st.s, st.ti, Zy);
                 ++r.rebases;
+                ++wz;
                 continue;
             }
         }
@@ -689,13 +805,16 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 st.ti *= sc;
                 st.e += k;
                 refresh_scale(st, dcf_r, dcf_i, dce);
+                zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                zi = Mant<T>::fma_(st.s, st.ti, Zy);
             }
         }
+        ++wz;
     }
     r.mag = (float)magT;
     r.m = m;
     r.wz = wz;
-    if (wz > p.depth) {
+    if (!blocked && wz > p.depth) {
         count = 0;
         return 1;
     }
@@ -718,7 +837,8 @@ __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double d
     PixRun<T> r;
     pixel_start(r, dcm_r, dcm_i, dce);
     uint32_t count = 0;
-    const int done = perturb_run<T, STREAM>(p, r, dcm_r, dcm_i, dce, p.depth, count, view);
+    const int done = perturb_run<T, STREAM ? kOrbitWait : kOrbitComplete>(p, r, dcm_r, dcm_i, dce,
+                                                                          p.depth, count, view);
     mag_out = r.mag;
     rebases += r.rebases;
     lost += r.lost;
@@ -949,8 +1069,8 @@ __global__ void __launch_bounds__(256, 5) serve_perturb_kernel(ServeDev* __restr
                     load_run(r, sp, dcm_r, dcm_i, p.hs_e);
                 const uint32_t last = r.wz + d->ctl.budget[slot] - 1u;
                 uint32_t count = 0;
-                if (perturb_run<float, false>(p, r, dcm_r, dcm_i, p.hs_e, last, count, nullptr)
-                    == 1) {
+                if (perturb_run<float, kOrbitSnapshot>(p, r, dcm_r, dcm_i, p.hs_e, last, count,
+                                                       nullptr, orbit_snapshot(p)) == 1) {
                     p.out[pix] = (int32_t)count;
                     if (p.mag)
                         p.mag[pix] = r.mag;
@@ -968,6 +1088,128 @@ __global__ void __launch_bounds__(256, 5) serve_perturb_kernel(ServeDev* __restr
         queue_append(again, e & ~kEntryFresh, qout, qout_count);
         retire_pixels(done, slot, d->status.remaining);
     }
+}
+
+// ---- streamed orbit: pixels start while the orbit is being iterated ----
+
+// Block 0: the producer (64 threads); block 1: the finisher.  Launched
+// cooperatively (both blocks resident at once: the finisher waits, bounded,
+// on the producer's progress).
+__global__ void __launch_bounds__(256) orbit_stream_kernel(OrbitLaunch o, OrbitProgress g,
+                                                           int* producer_sm)
+{
+    if (blockIdx.x == 0) {
+        unsigned smid = 0;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        if (threadIdx.x == 0) {
+            if (o.sm_busy)
+                atomicAdd(o.sm_busy + smid % (unsigned)o.sm_words, 1);
+            *(volatile int*)producer_sm = (int)smid + 1;
+        }
+        if (threadIdx.x < 64)
+            orbit_produce(o, &g);
+        if (threadIdx.x == 0) {
+            *(volatile int*)producer_sm = 0;
+            if (o.sm_busy)
+                atomicSub(o.sm_busy + smid % (unsigned)o.sm_words, 1);
+        }
+        return;
+    }
+    orbit_finisher(o, g);
+}
+
+// One step of the FP32 pass of one frame over a compacted pixel queue:
+// entries in[0 .. n) (in == nullptr: entry i is pixel i, fresh), every pixel
+// iterates at most `budget` iterations or until it needs an orbit entry not
+// finished yet; unfinished pixels are appended to out.
+struct FrameStep {
+    const unsigned* in;
+    unsigned n;
+    unsigned* out;
+    unsigned* out_count;
+    unsigned* pull;
+    unsigned* workers;   // blocks working this launch
+    uint4* state;        // 32 bytes per pixel
+    unsigned budget;
+};
+
+template <bool WANT_MAG>
+__global__ void __launch_bounds__(256, 5) perturb_step_kernel(PerturbLaunch p, FrameStep q)
+{
+    // leave the orbit producer's SM to it, unless no other block works yet
+    // (a working block pulls until the queue is empty)
+    __shared__ int s_leave;
+    if (threadIdx.x == 0) {
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        const bool producer_here = *(volatile const int*)p.producer_sm == (int)smid + 1;
+        s_leave = producer_here && *(volatile const unsigned*)q.workers > 0u;
+        if (!s_leave)
+            atomicAdd(q.workers, 1u);
+    }
+    __syncthreads();
+    if (s_leave)
+        return;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0)
+            base = atomicAdd(q.pull, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= q.n)
+            break;
+        const unsigned i = base + lane;
+        const bool valid = i < q.n;
+        const unsigned e = valid ? (q.in ? q.in[i] : (i | kEntryFresh)) : 0u;
+        const unsigned pix = e & kEntryPixelMask;
+        bool again = false;
+        unsigned long long its = 0;
+        unsigned reb = 0;
+        if (valid) {
+            const int line = (int)(pix / (unsigned)p.W);
+            const int ix = (int)(pix - (unsigned)line * (unsigned)p.W);
+            const double dcm_r = (double)(2 * ix - p.W) * p.hs_m;
+            const double dcm_i = (double)(p.H - 2 * (p.row0 + line)) * p.hs_m;
+            uint4* sp = q.state + (size_t)pix * 2u;
+            PixRun<float> r;
+            if (e & kEntryFresh)
+                pixel_start(r, dcm_r, dcm_i, p.hs_e);
+            else
+                load_run(r, sp, dcm_r, dcm_i, p.hs_e);
+            const uint32_t last = r.wz + q.budget - 1u;
+            uint32_t count = 0;
+            if (perturb_run<float, kOrbitSnapshot>(p, r, dcm_r, dcm_i, p.hs_e, last, count,
+                                                   nullptr, orbit_snapshot(p)) == 1) {
+                p.out[pix] = (int32_t)count;
+                if (WANT_MAG)
+                    p.mag[pix] = r.mag;
+                if (r.lost > p.lost_limit && p.flag_out)
+                    p.flag_out[atomicAdd(p.flag_out_count, 1u)] = pix;
+                else
+                    its = count ? count : p.depth;
+                reb = r.rebases;
+            } else {
+                store_run(r, sp);
+                again = true;
+            }
+        }
+        queue_append(again, pix, q.out, q.out_count);
+        its = warp_sum_u64(its);
+        const unsigned long long rb = warp_sum_u64((unsigned long long)reb);
+        if (lane == 0) {
+            if (its)
+                atomicAdd(&p.sync->iter_sum, its);
+            if (rb)
+                atomicAdd(p.rebases, rb);
+        }
+    }
+}
+
+__global__ void frame_step_reset_kernel(unsigned* counters)
+{
+    counters[0] = 0u;   // pull
+    counters[1] = 0u;   // out count
+    counters[2] = 0u;   // workers
 }
 
 __global__ void serve_enqueue_kernel(ServeDev* d, int cls, int q, int slot, unsigned npix)
@@ -1024,6 +1266,52 @@ int launch_serve_enqueue(ServeDev* d, int cls, int q, int slot, unsigned npix, c
 int launch_serve_step_end(ServeDev* d, cudaStream_t s)
 {
     serve_step_end_kernel<<<1, 32, 0, s>>>(d);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
+int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s)
+{
+    if (o.limbs < 5 || o.limbs > kMaxOrbitLimbs) {
+        set_error("orbit: %d limbs outside [5, %d]", o.limbs, kMaxOrbitLimbs);
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    OrbitLaunch oo = o;
+    OrbitProgress g{progress + 1, progress + 2, progress + 3, progress + 4};
+    int* producer_sm = progress + 5;
+    void* args[] = {&oo, &g, &producer_sm};
+    MDZ_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)orbit_stream_kernel, dim3(2), dim3(256),
+                                             args, 0, s));
+    return MDZGPU_OK;
+}
+
+int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in, unsigned n,
+                        unsigned* out, unsigned* counters, uint4* state, unsigned budget,
+                        cudaStream_t s)
+{
+    const bool mag = p.mag != nullptr;
+    const void* fn = mag ? (const void*)perturb_step_kernel<true>
+                         : (const void*)perturb_step_kernel<false>;
+    static int bps[2] = {0, 0};
+    int& b = bps[mag ? 1 : 0];
+    if (!b) {
+        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, 0));
+        if (b < 1)
+            b = 1;
+    }
+    long grid = (long)num_sms * b;
+    const long needed = ((long)n + 255) / 256;
+    if (grid > needed)
+        grid = needed;
+    if (grid < 1)
+        grid = 1;
+    frame_step_reset_kernel<<<1, 1, 0, s>>>(counters);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    FrameStep q{in, n, out, counters + 1, counters, counters + 2, state, budget};
+    if (mag)
+        perturb_step_kernel<true><<<(unsigned)grid, 256, 0, s>>>(p, q);
+    else
+        perturb_step_kernel<false><<<(unsigned)grid, 256, 0, s>>>(p, q);
     MDZ_CUDA_TRY(cudaGetLastError());
     return MDZGPU_OK;
 }

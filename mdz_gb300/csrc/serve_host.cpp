@@ -103,7 +103,7 @@ private:
     std::map<size_t, size_t> free_;
 };
 
-enum Phase { kQueued, kOrbit, kRunning, kFinishing, kEnded };
+enum Phase { kQueued, kRunning, kFinishing, kEnded };
 
 // Offsets of a request's pieces in its device block and its pinned block.
 struct Layout {
@@ -142,6 +142,8 @@ struct Req {
     double t_submit = 0, t_admit = 0, t_done = 0;
     int64_t pixel_iters = 0, esc_fp64 = 0, esc_mp = 0, rebases = 0, steps = 0;
     cudaEvent_t ev_orbit = nullptr, ev_done = nullptr;
+    bool orbit_running = false;  // streamed orbit not yet complete
+    bool cancelled = false;      // finishing only to release the memory
 };
 
 Layout make_layout(const Req& r)
@@ -651,6 +653,12 @@ int Server::setup(const std::shared_ptr<Req>& r)
         p.lost_limit = 1.0f;  // bits a pixel may lose before its FP64 re-run
         p.flag_out = (unsigned*)(db + l.lists + 256);
         p.flag_out_count = (unsigned*)(db + l.lists);
+        // progress of the streamed orbit (beside out_len, zeroed above)
+        int* prog = (int*)(ob + ol.len);
+        p.raw_len = prog + 1;
+        p.fin_len = prog + 2;
+        p.orbit_done = prog + 3;
+        p.orbit_error = prog + 4;
         q.state_stride = 2;
         MDZ_CUDA_TRY(cudaMemcpyAsync(&d->req[r->slot], &q, sizeof q, cudaMemcpyHostToDevice,
                                      main));
@@ -673,12 +681,23 @@ int Server::setup(const std::shared_ptr<Req>& r)
         cudaEventRecord(ready, main);
         cudaStreamWaitEvent(side[r->slot], ready, 0);
         cudaEventDestroy(ready);
-        int rc = launch_orbit(o, side[r->slot]);
+        // the orbit streams: pixels join the queue now and iterate up to
+        // the last finished entry at every step
+        int rc = launch_orbit_stream(o, prog, side[r->slot]);
         if (rc)
             return rc;
+        MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_misc + 16, prog + 4, 4, cudaMemcpyDeviceToHost,
+                                     side[r->slot]));
         MDZ_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_orbit, cudaEventDisableTiming));
         MDZ_CUDA_TRY(cudaEventRecord(r->ev_orbit, side[r->slot]));
-        r->phase = kOrbit;
+        rc = launch_serve_enqueue(d, 0, (int)cur, r->slot, (unsigned)r->npix, main);
+        if (rc)
+            return rc;
+        qhost[0] += (long)r->npix;
+        r->orbit_running = true;
+        r->phase = kRunning;
+        std::lock_guard<std::mutex> lk(mu);
+        st.launches += 3;
     } else {
         q.state_stride = serve_mp_state_stride(r->words);
         MDZ_CUDA_TRY(cudaMemcpyAsync(&d->req[r->slot], &q, sizeof q, cudaMemcpyHostToDevice,
@@ -697,37 +716,23 @@ int Server::setup(const std::shared_ptr<Req>& r)
 void Server::poll_orbits()
 {
     for (auto& r : slots) {
-        if (!r || r->phase != kOrbit)
+        if (!r || !r->orbit_running)
             continue;
         const cudaError_t e = cudaEventQuery(r->ev_orbit);
         if (e == cudaErrorNotReady)
             continue;
-        if (e != cudaSuccess) {
-            set_error("serve: reference orbit failed: %s", cudaGetErrorString(e));
-            auto keep = r;
-            end(keep, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
-            continue;
-        }
-        bool cancel;
-        {
+        r->orbit_running = false;
+        const int err = e != cudaSuccess
+                            ? 1
+                            : *(volatile int*)(stage_host + r->host_off + r->lay.h_misc + 16);
+        if (err) {
+            // the finisher gave up (or the launch failed): its pixels can not
+            // finish; drop them and fail the request
+            set_error("serve: reference orbit of request %lld failed", (long long)r->id);
             std::lock_guard<std::mutex> lk(mu);
-            cancel = r->cancel;
-            st.launches += 2;  // orbit + finish kernels
+            r->cancel = true;
+            r->cancel_state = MDZGPU_REQ_FAILED;
         }
-        if (cancel) {
-            auto keep = r;
-            end(keep, keep->cancel_state, 0);
-            continue;
-        }
-        if (launch_serve_enqueue(d, 0, (int)cur, r->slot, (unsigned)r->npix, main)) {
-            auto keep = r;
-            end(keep, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
-            continue;
-        }
-        qhost[0] += (long)r->npix;
-        r->phase = kRunning;
-        std::lock_guard<std::mutex> lk(mu);
-        st.launches += 2;
     }
 }
 
@@ -792,7 +797,16 @@ int Server::step()
             cancel = r->cancel;
         }
         if (cancel) {
-            end(r, r->cancel_state, 0);
+            // the slot stream may still run the orbit: release the memory
+            // once it is idle
+            r->cancelled = true;
+            if (cudaEventCreateWithFlags(&r->ev_done, cudaEventDisableTiming) != cudaSuccess
+                || cudaEventRecord(r->ev_done, side[r->slot]) != cudaSuccess) {
+                cudaStreamSynchronize(side[r->slot]);
+                end(r, r->cancel_state, 0);
+            } else {
+                r->phase = kFinishing;
+            }
             continue;
         }
         const int rc = start_finish(r);
@@ -886,6 +900,10 @@ void Server::poll_finishing()
             end(r, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
             continue;
         }
+        if (r->cancelled) {
+            end(r, r->cancel_state, 0);
+            continue;
+        }
         const Layout& l = r->lay;
         const char* hb = stage_host + r->host_off;
         const int32_t* c = (const int32_t*)(hb + l.h_counts);
@@ -947,7 +965,7 @@ void Server::run()
         if (queued == 0) {
             bool waiting_gpu = false;
             for (const auto& s : slots)
-                waiting_gpu = waiting_gpu || (s && (s->phase == kOrbit || s->phase == kFinishing));
+                waiting_gpu = waiting_gpu || (s && (s->orbit_running || s->phase == kFinishing));
             if (waiting_gpu)
                 std::this_thread::sleep_for(std::chrono::microseconds(100));
         }

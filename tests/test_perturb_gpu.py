@@ -116,3 +116,27 @@ def test_reference_orbit_matches_exact(renderer, cx, cy, prec, n):
         got_d = float(Fraction(dm[k]) * Fraction(2) ** int(de[k]))
         assert abs(got_d - d) <= 1e-9 * max(1e-300, abs(d)) + 2.0 ** -40, k
         xr, xi = (xr * xr - xi * xi) // 2 ** F + CR, (2 * xr * xi) // 2 ** F + CI
+
+
+@pytest.mark.parametrize("name", ["p_gal_polyp", "p_mis_b_1000", "p_gal_honeytrace",
+                                  "p_gal_spiralblues"])
+def test_perturb_schedules_agree(renderer, name, monkeypatch):
+    """The three pass-0 schedules (streamed orbit with compacting steps, the
+    orbit then one frame launch, the fused cooperative grid) give the same
+    counts and |z|^2 bit for bit: the pixel loop is one function whose state
+    can be saved and resumed at any iteration."""
+    m = META[name]
+    prec = m["prec"]
+    args = (m["W"] * 2, m["H"] * 2, m["depth"],
+            MpVal.from_fraction(parse_number(m["cx"]), prec),
+            MpVal.from_fraction(parse_number(m["cy"]), prec),
+            MpVal.from_fraction(parse_number(m["width"]) * 2, prec), prec)
+    out = {}
+    for mode in ("steps", "frame", "fused"):
+        monkeypatch.setenv("MDZGPU_PERTURB", mode)
+        counts, mag, st = renderer.render_perturb(*args, want_mag=True)
+        out[mode] = (counts, mag.view(np.uint32), st)
+    for mode in ("frame", "fused"):
+        assert np.array_equal(out[mode][0], out["steps"][0]), mode
+        assert np.array_equal(out[mode][1], out["steps"][1]), mode
+        assert out[mode][2]["pixel_iters"] == out["steps"][2]["pixel_iters"], mode
