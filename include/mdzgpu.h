@@ -125,6 +125,9 @@ typedef struct mdzgpu_stats {
     int64_t orbit_len;      /* reference orbit length (perturbation) */
     int64_t escalated_fp64; /* pixels re-run with FP64 deltas (perturbation) */
     int64_t escalated_mp;   /* pixels re-run on the multi-limb kernel */
+    double pixel_ms;        /* device time of the FP32 pixel-pass launches
+                               alone (perturbation; events around each) */
+    int64_t pixel_launches; /* FP32 pixel-pass launches (perturbation) */
 } mdzgpu_stats;
 
 /* An arbitrary-precision binary value with MPFR's meaning:

@@ -212,7 +212,9 @@ mdzgpu_ctx* mdzgpu_create(int device)
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess
         || cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess
         || cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess
-        || cudaEventCreate(&ctx->ev_side0) != cudaSuccess) {
+        || cudaEventCreate(&ctx->ev_side0) != cudaSuccess
+        || cudaEventCreate(&ctx->ev_k0) != cudaSuccess
+        || cudaEventCreate(&ctx->ev_k1) != cudaSuccess) {
         set_error("stream/event creation failed");
         delete ctx;
         return nullptr;
@@ -242,6 +244,8 @@ void mdzgpu_destroy(mdzgpu_ctx* ctx)
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
     cudaEventDestroy(ctx->ev_side0);
+    cudaEventDestroy(ctx->ev_k0);
+    cudaEventDestroy(ctx->ev_k1);
     cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -552,7 +556,7 @@ namespace mdz {
 OrbitLayout orbit_layout(size_t entries, int L)
 {
     // zf[entries] float2 | zd[entries] double2 | ze[entries] int |
-    // dd[entries] double | de[entries] int | len + progress words |
+    // dd[entries] double | de[entries] int | tiny bits | len + progress words |
     // centre digits | rebases | digits[entries][2][L] int (raw orbit, scratch)
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     OrbitLayout o;
@@ -560,7 +564,8 @@ OrbitLayout orbit_layout(size_t entries, int L)
     o.ze = o.zd + al(entries * sizeof(double2));
     o.dd = o.ze + al(entries * sizeof(int));
     o.de = o.dd + al(entries * sizeof(double));
-    o.len = o.de + al(entries * sizeof(int));
+    o.tiny = o.de + al(entries * sizeof(int));
+    o.len = o.tiny + al((entries / 32 + 40) * sizeof(unsigned));  // + whole last batches
     o.dig = o.len + 256;
     o.reb = o.dig + al(2 * (size_t)L * sizeof(int));
     o.raw = o.reb + 256;
@@ -620,7 +625,8 @@ extern "C" {
 // finished orbit entry; the unfinished ones are compacted into the other
 // queue.  The budget keeps one step near 8 ms of GPU time.
 static int perturb_steps(mdzgpu_ctx* ctx, const PerturbLaunch& p, size_t n,
-                         cudaEvent_t orbit_done_ev, int* launches)
+                         cudaEvent_t orbit_done_ev, int* launches, double* pixel_ms,
+                         int64_t* pixel_launches)
 {
     int rc;
     if ((rc = ctx->pstate.ensure(n * 32)) || (rc = ctx->pqueue.ensure(2 * n * 4 + 256))
@@ -643,11 +649,16 @@ static int perturb_steps(mdzgpu_ctx* ctx, const PerturbLaunch& p, size_t n,
         const double b = rate * 8e-3 / (double)left;
         const unsigned budget = (unsigned)std::min(std::max(b, 256.0), (double)(1u << 24));
         if ((rc = launch_perturb_step(ctx->num_sms, p, in, left, out, counters,
-                                      (uint4*)ctx->pstate.ptr, budget, ctx->stream)))
+                                      (uint4*)ctx->pstate.ptr, budget, ctx->stream, ctx->ev_k0,
+                                      ctx->ev_k1)))
             return rc;
         MDZ_CUDA_TRY(cudaMemcpyAsync((void*)h_count, counters + 1, 4, cudaMemcpyDeviceToHost,
                                      ctx->stream));
         MDZ_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        float kms = 0.f;
+        MDZ_CUDA_TRY(cudaEventElapsedTime(&kms, ctx->ev_k0, ctx->ev_k1));
+        *pixel_ms += kms;
+        ++*pixel_launches;
         *launches += 2;
         left = *h_count;
         if (left == 0)
@@ -744,6 +755,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.digits = (int*)(ob + off_raw);
     o.max_k = (int)f->depth + 1;
     o.out_len = (int*)(ob + off_len);
+    o.tiny = (unsigned*)(ob + ol.tiny);
     int64_t h2d_extra = 0;
     cudaEvent_t evo;
     MDZ_CUDA_TRY(cudaEventCreate(&evo));
@@ -797,6 +809,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.dd = o.dd;
     p.de = o.de;
     p.orbit_len = o.out_len;
+    p.tiny = o.tiny;
     p.out = d_out;
     p.mag = d_mag;
     p.sync = (FrameSync*)ctx->sync.ptr;
@@ -822,8 +835,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.orbit_error = prog + 4;
     p.producer_sm = prog + 5;
     int launches = 5;
+    double pixel_ms = 0.0;
+    int64_t pixel_launches = 0;
     if (stepped) {
-        rc = perturb_steps(ctx, p, n, evo, &launches);
+        rc = perturb_steps(ctx, p, n, evo, &launches, &pixel_ms, &pixel_launches);
         // the list passes read the whole orbit
         if (!rc && cudaStreamWaitEvent(ctx->stream, evo, 0) != cudaSuccess)
             rc = MDZGPU_ERR_CUDA;
@@ -920,6 +935,8 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         st->orbit_ms = fused ? -1.0 : oms;
         st->rebases = (int64_t)reb;
         st->orbit_len = olen;
+        st->pixel_ms = pixel_ms;
+        st->pixel_launches = pixel_launches;
     }
     cudaEventDestroy(evo);
     return rc;

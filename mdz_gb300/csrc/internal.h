@@ -59,6 +59,7 @@ struct mdzgpu_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;   // high priority: the streamed orbit
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_side0 = nullptr;
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // around one pixel-pass launch
     mdz::DevBuf counts;     // int32 counts
     mdz::DevBuf sync;       // FrameSync + tile-row counters
     mdz::DevBuf coords;     // fixed-point pixel coordinates (MP path)
@@ -130,6 +131,7 @@ struct OrbitLaunch {
     int* out_len;           // number of valid entries (device)
     int* sm_busy = nullptr; // serving: producers per SM id (counted while running)
     int sm_words = 0;
+    unsigned* tiny = nullptr;  // [max_k / 32 + 2] bit k: |Z_k|^2 < 2^-120 (FP32)
 };
 int launch_orbit(const OrbitLaunch& p, cudaStream_t s);
 int orbit_max_limbs();
@@ -145,6 +147,7 @@ struct PerturbLaunch {
     const double* dd;
     const int* de;
     const int* orbit_len;   // device: valid orbit entries
+    const unsigned* tiny;   // bit mask of tiny |Z_k| (see OrbitLaunch)
     int32_t* out;
     float* mag;             // |z|^2 at escape (may be null)
     FrameSync* sync;
@@ -179,7 +182,8 @@ int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s);
 // placed on the orbit producer's SM (p.producer_sm) leave it to the producer.
 int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in, unsigned n,
                         unsigned* out, unsigned* counters, uint4* state, unsigned budget,
-                        cudaStream_t s);
+                        cudaStream_t s, cudaEvent_t before = nullptr,
+                        cudaEvent_t after = nullptr);
 // Orbit + FP32 pixel pass in one cooperative launch (progress words in p).
 int launch_fused(mdzgpu_ctx* ctx, const OrbitLaunch& o, const PerturbLaunch& p, cudaStream_t s);
 
@@ -212,7 +216,7 @@ int mpfr_round_to_fixed(const mdzgpu_mpval* v, long p, int words, uint32_t* out)
 // Reference-orbit buffer: byte offsets of its 256-byte aligned pieces for
 // `entries` entries of L digits (zf at 0).
 struct OrbitLayout {
-    size_t zd, ze, dd, de, len, dig, reb, raw, bytes;
+    size_t zd, ze, dd, de, tiny, len, dig, reb, raw, bytes;
 };
 OrbitLayout orbit_layout(size_t entries, int L);
 // Multi-limb word count of the perturbation's last escalation pass.

@@ -279,7 +279,8 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
         p.zd[k] = make_double2(vr, vi);
         p.ze[k] = 0;
     }
-    p.zf[k] = make_float2((float)vr, (float)vi);
+    const float2 zf = make_float2((float)vr, (float)vi);
+    p.zf[k] = zf;
     const double d_approx = vr * vr + vi * vi - 4.0;
     if (fabs(d_approx) > 9.5367431640625e-7 /* 2^-20 */) {
         p.dd[k] = d_approx;
@@ -318,17 +319,34 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
     p.de[k] = x;
 }
 
+// Bit k of p.tiny: |Z_k|^2 < 2^-120 in FP32 (the pixel pass takes the full
+// floatexp step there when dz is below the FP32 range).  Written per warp of
+// 32 consecutive entries, so every word has one writer.
+__device__ __forceinline__ void write_tiny_bits(const OrbitLaunch& p, int k, bool valid)
+{
+    bool tiny = false;
+    if (valid) {
+        const float2 z = p.zf[k];
+        tiny = fmaf(z.x, z.x, z.y * z.y) < 7.5e-37f;
+    }
+    const unsigned bits = __ballot_sync(0xffffffffu, tiny);
+    if (p.tiny && (threadIdx.x & 31) == 0 && k >= 0)
+        p.tiny[k >> 5] = bits;
+}
+
 __global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < *p.out_len)
+    const bool valid = k < *p.out_len;
+    if (valid)
         finish_entry(p, k, false);
+    write_tiny_bits(p, k, valid);
 }
 
-// The finisher of the fused launch (one block of 256 threads): finishes the
-// orbit in batches of 256 entries as the producer publishes them and
-// publishes fin_len in whole batches, so a consumer never reads a cache line
-// holding an unfinished entry.
+// The finisher of the streamed orbit (one block of 256 threads): finishes
+// the orbit in batches of 256 entries as the producer publishes them and
+// publishes fin_len in units of 1024 entries, so a consumer never reads a
+// cache line holding an unfinished entry.
 __device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
 {
     __shared__ int s_avail, s_done, s_err;
@@ -362,9 +380,13 @@ __device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
         const int k = fin + (int)threadIdx.x;
         if (k < end)
             finish_entry(p, k, true);
+        write_tiny_bits(p, k, k < end);
         __threadfence();
         __syncthreads();
-        if (threadIdx.x == 0)
+        // publish in whole 1024-entry units (one 128-byte line of the tiny
+        // mask, eight lines of zf) or at the end, so that no cache line a
+        // consumer reads holds an entry that is not finished yet
+        if (threadIdx.x == 0 && ((end & 1023) == 0 || (dn && end >= avail)))
             *(volatile int*)g.fin_len = end;
         fin = end;
         if (dn && fin >= avail)
@@ -517,6 +539,28 @@ __device__ __forceinline__ bool escape_exact(const PerturbLaunch& p, int m, cons
     const int E = max(max(dexp_of(dd) + de, dexp_of(t2) + e2), dexp_of(t3) + e3);
     const double v = ldexp(dd, de - E) + ldexp(t2, e2 - E) + ldexp(t3, e3 - E);
     return v > 0.0;
+}
+
+// |Z_m|^2 below the FP32 range of the dz^2 term (the slow-step trigger):
+// FP32 reads the orbit's bit mask, FP64 tests the value itself.
+template <class T>
+__device__ __forceinline__ bool z_tiny(const PerturbLaunch& p, int m, T zx, T zy)
+{
+    if (sizeof(T) == 4)
+        return (__ldg(p.tiny + (m >> 5)) >> (m & 31)) & 1u;
+    return zx * zx + zy * zy < (T)Mant<T>::kTinyZ2;
+}
+
+// True when none of Z_m .. Z_{m+3} is tiny (FP32 bit mask).  The next word
+// is read only when bits m .. m+3 reach into it: a word holding no entry
+// below the orbit progress must not be loaded (the finisher publishes whole
+// 128-byte lines of the mask, and a line loaded early would stay stale in
+// this SM's L1 for the rest of the launch).
+__device__ __forceinline__ bool four_not_tiny(const PerturbLaunch& p, int m)
+{
+    const unsigned lo = __ldg(p.tiny + (m >> 5));
+    const unsigned hi = ((unsigned)m & 31u) > 28u ? __ldg(p.tiny + (m >> 5) + 1) : 0u;
+    return (__funnelshift_r(lo, hi, (unsigned)m & 31u) & 0xfu) == 0u;
 }
 
 template <class T>
@@ -706,7 +750,11 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
     bool blocked = false;
     while (wz <= last) {
         bool attention = false;
-        if ((wz & 3u) == 1u && wz + 3u <= last && m + 4 < avail && !st.careful) {
+        // blocks: FP32 (the FP64 pass is the rare escalation path), no
+        // slow step among the four (dz below the FP32 range needs one only
+        // where Z_m is tiny)
+        if (sizeof(T) == 4 && (wz & 3u) == 1u && wz + 3u <= last && m + 4 < avail
+            && !st.force_slow && (!st.slow_if_tiny || four_not_tiny(p, m))) {
             // iterations wz .. wz+3, orbit entries m+1 .. m+4 all finished
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -760,7 +808,7 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                     ++r.rebases;
                 }
             }
-            if (st.careful && (st.force_slow || Zx * Zx + Zy * Zy < (T)Mant<T>::kTinyZ2)) {
+            if (st.careful && (st.force_slow || z_tiny<T>(p, m, Zx, Zy))) {
                 slow_step<T>(p, m, st, dcf_r, dcf_i, dcm_r, dcm_i, dce);
             } else {
                 fast_step<T>(st, Zx, Zy, zr, zi);
@@ -1287,7 +1335,7 @@ int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s)
 
 int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in, unsigned n,
                         unsigned* out, unsigned* counters, uint4* state, unsigned budget,
-                        cudaStream_t s)
+                        cudaStream_t s, cudaEvent_t before, cudaEvent_t after)
 {
     const bool mag = p.mag != nullptr;
     const void* fn = mag ? (const void*)perturb_step_kernel<true>
@@ -1308,11 +1356,15 @@ int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in,
     frame_step_reset_kernel<<<1, 1, 0, s>>>(counters);
     MDZ_CUDA_TRY(cudaGetLastError());
     FrameStep q{in, n, out, counters + 1, counters, counters + 2, state, budget};
+    if (before)
+        MDZ_CUDA_TRY(cudaEventRecord(before, s));
     if (mag)
         perturb_step_kernel<true><<<(unsigned)grid, 256, 0, s>>>(p, q);
     else
         perturb_step_kernel<false><<<(unsigned)grid, 256, 0, s>>>(p, q);
     MDZ_CUDA_TRY(cudaGetLastError());
+    if (after)
+        MDZ_CUDA_TRY(cudaEventRecord(after, s));
     return MDZGPU_OK;
 }
 

@@ -649,6 +649,7 @@ int Server::setup(const std::shared_ptr<Req>& r)
         p.dd = (const double*)(ob + ol.dd);
         p.de = (const int*)(ob + ol.de);
         p.orbit_len = (const int*)(ob + ol.len);
+        p.tiny = (const unsigned*)(ob + ol.tiny);
         p.rebases = (unsigned long long*)(ob + ol.reb);
         p.lost_limit = 1.0f;  // bits a pixel may lose before its FP64 re-run
         p.flag_out = (unsigned*)(db + l.lists + 256);
@@ -674,6 +675,7 @@ int Server::setup(const std::shared_ptr<Req>& r)
         o.digits = (int*)(ob + ol.raw);
         o.max_k = (int)r->depth + 1;
         o.out_len = (int*)(ob + ol.len);
+        o.tiny = (unsigned*)(ob + ol.tiny);
         o.sm_busy = d->sm_busy;
         o.sm_words = kServeSmWords;
         cudaEvent_t ready;

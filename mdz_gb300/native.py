@@ -28,7 +28,8 @@ class Stats(C.Structure):
                 ("pixel_iters", C.c_int64), ("h2d_bytes", C.c_int64),
                 ("d2h_bytes", C.c_int64), ("launches", C.c_int32), ("words", C.c_int32),
                 ("orbit_ms", C.c_double), ("rebases", C.c_int64), ("orbit_len", C.c_int64),
-                ("escalated_fp64", C.c_int64), ("escalated_mp", C.c_int64)]
+                ("escalated_fp64", C.c_int64), ("escalated_mp", C.c_int64),
+                ("pixel_ms", C.c_double), ("pixel_launches", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
