@@ -38,6 +38,7 @@ namespace {
 constexpr int kTileW = 8;
 constexpr int kTileH = 4;
 constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
+constexpr int kOrbitThreads = 128;  // producer threads (four warps)
 // Bounded waits of the fused launch: ~2^25 polls of >= 256 ns (several
 // seconds), far beyond any legitimate wait, then the error flag is raised.
 constexpr int kSpinLimit = 1 << 25;
@@ -94,17 +95,23 @@ struct OrbitProgress {
     int* error;     // a bounded wait gave up
 };
 
-// The producer, run by 64 threads (threadIdx.x < 64) with named barrier 1;
-// publishes raw_len every 32 steps when `prog` is given.
+// The producer, run by kOrbitThreads = 128 threads (threadIdx.x < 128) with
+// named barrier 1: warp w computes part w & 1 (0: Re, 1: Im) over half
+// w >> 1 of every column's terms; the second halves' partial sums meet the
+// first halves' in shared memory, whose warps then resolve the carries and
+// write Z_{k+1}.  Publishes raw_len every 32 steps when `prog` is given.
 __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProgress* prog)
 {
     __shared__ int2 z[kMaxOrbitLimbs];
     __shared__ int cc[2][kMaxOrbitLimbs];
-    auto bar = [] { asm volatile("bar.sync 1, 64;" ::: "memory"); };
+    __shared__ long long partial[2][3][32];
+    auto bar = [] { asm volatile("bar.sync 1, 128;" ::: "memory"); };
     const int lane = threadIdx.x & 31;
-    const int part = threadIdx.x >> 5;  // 0: real, 1: imaginary
+    const int warp = threadIdx.x >> 5;
+    const int part = warp & 1;   // 0: real, 1: imaginary
+    const int half = warp >> 1;  // which half of each column's terms
     const int L = p.limbs;
-    for (int j = threadIdx.x; j < L; j += 64) {
+    for (int j = threadIdx.x; j < L; j += kOrbitThreads) {
         cc[0][j] = p.c_re[j];
         cc[1][j] = p.c_im[j];
         z[j] = make_int2(p.c_re[j], p.c_im[j]);
@@ -142,10 +149,12 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
             const int c = cbase + lane + 32 * s;
             if (s >= nslots || c > ctop)
                 continue;
-            const int ilo = c - (L - 1) > 0 ? c - (L - 1) : 0;
-            const int ihi = (c - 1) >> 1;  // i < j = c - i
+            const int lo = c - (L - 1) > 0 ? c - (L - 1) : 0;
+            const int hi = (c - 1) >> 1;  // i < j = c - i
+            const int mid = lo + (hi - lo + 2) / 2;
+            int i = half ? mid : lo;
+            const int ihi = half ? hi : mid - 1;
             long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-            int i = ilo;
             if (part == 0) {
                 for (; i + 3 <= ihi; i += 4) {
                     const int j = c - i;
@@ -176,15 +185,28 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
                 }
             }
             long long acc = 2 * ((a0 + a1) + (a2 + a3));
-            if (!(c & 1)) {
-                const int2 h = z[c >> 1];
-                acc += part == 0 ? (long long)h.x * h.x - (long long)h.y * h.y
-                                 : 2 * (long long)h.x * h.y;
+            if (!half) {
+                if (!(c & 1)) {
+                    const int2 h = z[c >> 1];
+                    acc += part == 0 ? (long long)h.x * h.x - (long long)h.y * h.y
+                                     : 2 * (long long)h.x * h.y;
+                }
+                if (c >= L - 1)
+                    acc += cpart[c - (L - 1)];
             }
-            if (c >= L - 1)
-                acc += cpart[c - (L - 1)];
             v[s] = acc;
         }
+        if (half) {
+#pragma unroll
+            for (int s = 0; s < 3; ++s)
+                partial[part][s][lane] = v[s];
+        }
+        bar();  // partial sums in place; every read of Z_k done
+        if (half)
+            continue;
+#pragma unroll
+        for (int s = 0; s < 3; ++s)
+            v[s] += partial[part][s][lane];
         // carry propagation: column c+1 is lane+1 (slot s) or lane 0 of
         // slot s+1; two passes bound every digit by 2^27 + 2^5
 #pragma unroll
@@ -204,7 +226,6 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
                 v[s] = dg[s] + in;
             }
         }
-        bar();  // every read of Z_k done
         int* out = p.digits + (size_t)(k + 1) * 2 * L + part * L;
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
@@ -231,7 +252,7 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
     }
 }
 
-__global__ void __launch_bounds__(64) orbit_kernel(OrbitLaunch p)
+__global__ void __launch_bounds__(kOrbitThreads) orbit_kernel(OrbitLaunch p)
 {
     // serving: the slice kernels keep their blocks off an SM while a
     // producer runs there, so its latency-bound warps own the issue slots
@@ -997,7 +1018,7 @@ __global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, Pe
         if (threadIdx.x == 0)
             *(volatile int*)p.producer_sm = (int)smid + 1;
         OrbitProgress g{p.raw_len, p.fin_len, p.orbit_done, p.orbit_error};
-        if (threadIdx.x < 64)
+        if (threadIdx.x < kOrbitThreads)
             orbit_produce(o, &g);
         return;
     }
@@ -1140,7 +1161,7 @@ __global__ void __launch_bounds__(256, 5) serve_perturb_kernel(ServeDev* __restr
 
 // ---- streamed orbit: pixels start while the orbit is being iterated ----
 
-// Block 0: the producer (64 threads); block 1: the finisher.  Launched
+// Block 0: the producer (128 threads); block 1: the finisher.  Launched
 // cooperatively (both blocks resident at once: the finisher waits, bounded,
 // on the producer's progress).
 __global__ void __launch_bounds__(256) orbit_stream_kernel(OrbitLaunch o, OrbitProgress g,
@@ -1154,7 +1175,7 @@ __global__ void __launch_bounds__(256) orbit_stream_kernel(OrbitLaunch o, OrbitP
                 atomicAdd(o.sm_busy + smid % (unsigned)o.sm_words, 1);
             *(volatile int*)producer_sm = (int)smid + 1;
         }
-        if (threadIdx.x < 64)
+        if (threadIdx.x < kOrbitThreads)
             orbit_produce(o, &g);
         if (threadIdx.x == 0) {
             *(volatile int*)producer_sm = 0;
@@ -1374,7 +1395,7 @@ int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
         set_error("orbit: %d limbs outside [5, %d]", p.limbs, kMaxOrbitLimbs);
         return MDZGPU_ERR_UNSUPPORTED;
     }
-    orbit_kernel<<<1, 64, 0, s>>>(p);
+    orbit_kernel<<<1, kOrbitThreads, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
     orbit_finish_kernel<<<(p.max_k + 1 + 127) / 128, 128, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
