@@ -555,12 +555,12 @@ namespace mdz {
 
 OrbitLayout orbit_layout(size_t entries, int L)
 {
-    // zf[entries] float2 | zd[entries] double2 | ze[entries] int |
+    // zq[entries] float4 | zd[entries] double2 | ze[entries] int |
     // dd[entries] double | de[entries] int | tiny bits | len + progress words |
     // centre digits | rebases | digits[entries][2][L] int (raw orbit, scratch)
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     OrbitLayout o;
-    o.zd = al(entries * sizeof(float2));
+    o.zd = al(entries * sizeof(float4));
     o.ze = o.zd + al(entries * sizeof(double2));
     o.dd = o.ze + al(entries * sizeof(int));
     o.de = o.dd + al(entries * sizeof(double));
@@ -747,7 +747,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.limbs = L;
     o.c_re = (const int*)(ob + off_dig);
     o.c_im = o.c_re + L;
-    o.zf = (float2*)ob;
+    o.zq = (float4*)ob;
     o.zd = (double2*)(ob + off_zd);
     o.ze = (int*)(ob + off_ze);
     o.dd = (double*)(ob + off_dd);
@@ -803,7 +803,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.depth = (uint32_t)f->depth;
     p.hs_m = hs_m;
     p.hs_e = hs_e;
-    p.zf = o.zf;
+    p.zq = o.zq;
     p.zd = o.zd;
     p.ze = o.ze;
     p.dd = o.dd;
@@ -963,7 +963,7 @@ int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx, const mdzgpu
     }
     const size_t entries = (size_t)max_k + 1;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t off_zd = al(entries * sizeof(float2));
+    const size_t off_zd = al(entries * sizeof(float4));
     const size_t off_ze = off_zd + al(entries * sizeof(double2));
     const size_t off_dd = off_ze + al(entries * sizeof(int));
     const size_t off_de = off_dd + al(entries * sizeof(double));
@@ -981,7 +981,7 @@ int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx, const mdzgpu
     o.limbs = L;
     o.c_re = (const int*)(ob + off_dig);
     o.c_im = o.c_re + L;
-    o.zf = (float2*)ob;
+    o.zq = (float4*)ob;
     o.zd = (double2*)(ob + off_zd);
     o.ze = (int*)(ob + off_ze);
     o.dd = (double*)(ob + off_dd);

@@ -122,7 +122,7 @@ struct OrbitLaunch {
     const int* c_re;        // [L] centre, balanced signed digits
     const int* c_im;
     int* digits;            // [max_k + 1][2][L] raw digits of every Z_k
-    float2* zf;             // [max_k + 1] Z_k in FP32
+    float4* zq;             // [max_k + 1] (Z_k re, im, |Z_k|^2, 0) in FP32
     double2* zd;            // [max_k + 1] Z_k mantissas in FP64 ...
     int* ze;                // ... times 2^ze[k]
     double* dd;             // [max_k + 1] D_k = |Z_k|^2 - 4 = dd * 2^de
@@ -141,7 +141,7 @@ struct PerturbLaunch {
     uint32_t depth;
     double hs_m;            // half pixel spacing = hs_m * 2^hs_e, <= 40 bits
     int hs_e;
-    const float2* zf;
+    const float4* zq;
     const double2* zd;
     const int* ze;
     const double* dd;

@@ -300,8 +300,9 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
         p.zd[k] = make_double2(vr, vi);
         p.ze[k] = 0;
     }
-    const float2 zf = make_float2((float)vr, (float)vi);
-    p.zf[k] = zf;
+    const float fx = (float)vr, fy = (float)vi;
+    // |Z_k|^2 exactly as the pixel loop forms |z|^2 when dz vanishes in FP32
+    p.zq[k] = make_float4(fx, fy, fmaf(fx, fx, fy * fy), 0.f);
     const double d_approx = vr * vr + vi * vi - 4.0;
     if (fabs(d_approx) > 9.5367431640625e-7 /* 2^-20 */) {
         p.dd[k] = d_approx;
@@ -347,8 +348,7 @@ __device__ __forceinline__ void write_tiny_bits(const OrbitLaunch& p, int k, boo
 {
     bool tiny = false;
     if (valid) {
-        const float2 z = p.zf[k];
-        tiny = fmaf(z.x, z.x, z.y * z.y) < 7.5e-37f;
+        tiny = p.zq[k].z < 7.5e-37f;
     }
     const unsigned bits = __ballot_sync(0xffffffffu, tiny);
     if (p.tiny && (threadIdx.x & 31) == 0 && k >= 0)
@@ -405,7 +405,7 @@ __device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
         __threadfence();
         __syncthreads();
         // publish in whole 1024-entry units (one 128-byte line of the tiny
-        // mask, eight lines of zf) or at the end, so that no cache line a
+        // mask, 128 lines of zq) or at the end, so that no cache line a
         // consumer reads holds an entry that is not finished yet
         if (threadIdx.x == 0 && ((end & 1023) == 0 || (dn && end >= avail)))
             *(volatile int*)g.fin_len = end;
@@ -588,7 +588,7 @@ template <class T>
 __device__ __forceinline__ void load_z(const PerturbLaunch& p, int m, T& zx, T& zy)
 {
     if (sizeof(T) == 4) {
-        const float2 z = p.zf[m];
+        const float4 z = p.zq[m];
         zx = (T)z.x;
         zy = (T)z.y;
     } else {
@@ -777,21 +777,46 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
         if (sizeof(T) == 4 && (wz & 3u) == 1u && wz + 3u <= last && m + 4 < avail
             && !st.force_slow && (!st.slow_if_tiny || four_not_tiny(p, m))) {
             // iterations wz .. wz+3, orbit entries m+1 .. m+4 all finished
+            if (st.s == (T)0) {
+                // dz below the FP32 range (deep zoom): s t and s t^2 vanish
+                // exactly, so the step is t' = 2 Z_m t + dc 2^-e, |z|^2 is
+                // |Z_m|^2 (stored with the entry, formed as below) and the
+                // rebase screen is |z| tiny -- the same values the general
+                // code computes with s = 0
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                fast_step<T>(st, Zx, Zy, zr, zi);
-                ++m;
-                load_z<T>(p, m, Zx, Zy);
-                zr = Mant<T>::fma_(st.s, st.tr, Zx);
-                zi = Mant<T>::fma_(st.s, st.ti, Zy);
-                magT = Mant<T>::fma_(zr, zr, zi * zi);
-                const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
-                if (magT > band_lo || Mant<T>::fma_(st.s2x4, dd, -magT) >= (T)0
-                    || magT < (T)Mant<T>::kGlitchZ2) {
-                    attention = true;
-                    break;
+                for (int u = 0; u < 4; ++u) {
+                    const T tr = st.tr, ti = st.ti;
+                    const T u2 = tr + tr, v2 = ti + ti;
+                    st.tr = Mant<T>::fma_(Zx, u2, Mant<T>::fma_(-Zy, v2, st.dcr));
+                    st.ti = Mant<T>::fma_(Zx, v2, Mant<T>::fma_(Zy, u2, st.dci));
+                    ++m;
+                    const float4 q = p.zq[m];
+                    Zx = (T)q.x;
+                    Zy = (T)q.y;
+                    magT = (T)q.z;
+                    if (magT > band_lo || magT < (T)Mant<T>::kGlitchZ2) {
+                        attention = true;
+                        break;
+                    }
+                    ++wz;
                 }
-                ++wz;
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    fast_step<T>(st, Zx, Zy, zr, zi);
+                    ++m;
+                    load_z<T>(p, m, Zx, Zy);
+                    zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                    zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                    magT = Mant<T>::fma_(zr, zr, zi * zi);
+                    const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
+                    if (magT > band_lo || Mant<T>::fma_(st.s2x4, dd, -magT) >= (T)0
+                        || magT < (T)Mant<T>::kGlitchZ2) {
+                        attention = true;
+                        break;
+                    }
+                    ++wz;
+                }
             }
             if (!attention) {
                 // wz - 1 = 4k + 4: the rescale check of the general path

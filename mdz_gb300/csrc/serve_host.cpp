@@ -643,7 +643,7 @@ int Server::setup(const std::shared_ptr<Req>& r)
         MDZ_CUDA_TRY(cudaMemsetAsync(ob + ol.len, 0, 256, main));
         MDZ_CUDA_TRY(cudaMemsetAsync(ob + ol.reb, 0, 256, main));
         MDZ_CUDA_TRY(cudaMemsetAsync(db + l.lists, 0, 256, main));
-        p.zf = (const float2*)ob;
+        p.zq = (const float4*)ob;
         p.zd = (const double2*)(ob + ol.zd);
         p.ze = (const int*)(ob + ol.ze);
         p.dd = (const double*)(ob + ol.dd);
@@ -667,7 +667,7 @@ int Server::setup(const std::shared_ptr<Req>& r)
         o.limbs = r->limbs;
         o.c_re = (const int*)(ob + ol.dig);
         o.c_im = o.c_re + r->limbs;
-        o.zf = (float2*)ob;
+        o.zq = (float4*)ob;
         o.zd = (double2*)(ob + ol.zd);
         o.ze = (int*)(ob + ol.ze);
         o.dd = (double*)(ob + ol.dd);

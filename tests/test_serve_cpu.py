@@ -30,7 +30,7 @@ def test_footprint_perturbation_layout():
     n = 100 * 60
     L = native.load().mdzgpu_perturb_limbs(300)
     entries = 5002
-    orbit = (al(entries * 8) + al(entries * 16) + al(entries * 4) + al(entries * 8)
+    orbit = (al(entries * 16) + al(entries * 16) + al(entries * 4) + al(entries * 8)
              + al(entries * 4) + al((entries // 32 + 40) * 4) + 256 + al(2 * L * 4) + 256
              + al(entries * 2 * L * 4))
     # counts, |z|^2, 32-byte pixel state, two escalation lists, sync, orbit
