@@ -16,6 +16,8 @@ Lines printed (rank 0, one JSON line):
   roofline  the perturbation kernel against the measured FP32 pipe peak;
   cpu_baseline  the oracle's MPFR loop (the reference's deep-zoom path at
             1088 bits) on a bounded pixel sample, all host threads;
+  plain_configs  config 2 (FP64) and config 3 (multi-limb) frames, each
+            beside the reference CPU loop on a band of rows;
   serving   the seeded mixed request stream (mdz_gb300.stream) through the
             serving engine: capacity (closed loop) and p50/p99 latency under
             Poisson arrivals at 80% of that capacity (rank 0).
@@ -61,6 +63,8 @@ def parse_args():
                     help="requests of the seeded mixed stream for the serving latency run "
                          "(0 = skip)")
     ap.add_argument("--serve-seed", type=int, default=5005)
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the config 2 (FP64) and config 3 (multi-limb) frames")
     ap.add_argument("--serve-load", type=float, default=0.8)
     ap.add_argument("--frame", default=None,
                     help="WxH override of the frame size (same centre, pixel spacing scaled) "
@@ -214,6 +218,71 @@ def run_reference(args, view, world, rank, dist):
             "e2e": {"value": value, "unit": "pixel-iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_plain_configs(args, local) -> dict:
+    """The plain methods on their own configurations, each beside the
+    reference's CPU loop (the oracle restatement, all host threads) on a band
+    of rows of the same frame: config 2 (FP64, 1920x1080 with 3x3
+    supersampling = 5760x3240 counts, maxiter 20000) and config 3 (multi-limb,
+    640x480 at 256 bits, maxiter 50000).  GPU numbers are the whole frame
+    through the public call with a host output buffer (counts copied back)."""
+    from mdz_gb300 import Renderer
+    from mdz_gb300.cases import view as case_view
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    out = {}
+    with Renderer(local) as r:
+        v = case_view("c2", None, aa=True)
+        xmin, xmax, ymax = v.rect().doubles()
+        W, H = v.real_width, v.real_height
+        r.render_fp64(W, 64, v.depth, xmin, xmax, ymax)              # warm-up
+        t0 = time.perf_counter()
+        _, st = r.render_fp64(W, H, v.depth, xmin, xmax, ymax)
+        wall = time.perf_counter() - t0
+        gpu = st["pixel_iters"] / wall
+        # CPU: rows from the middle of the frame, doubling until ~seconds
+        rows, cpu_its, cpu_s = 8, 0, 0.0
+        while cpu_s < args.cpu_seconds / 2 and rows <= H:
+            row0 = H // 2 - rows // 2
+            t0 = time.perf_counter()
+            band = O.render_fp64_rows(W, H, row0, rows, v.depth, xmin, xmax, ymax,
+                                      threads=threads)
+            cpu_s = time.perf_counter() - t0
+            cpu_its = int(np.where(band == 0, v.depth, band).sum())
+            rows *= 2
+        cpu = cpu_its / cpu_s
+        out["c2_fp64"] = {"value": gpu, "unit": "pixel-iters/s", "frame": f"{W}x{H}",
+                          "kernel_ms": st["kernel_ms"], "wall_ms": wall * 1e3,
+                          "cpu_baseline": {"value": cpu, "cores": threads, "kind": "port",
+                                           "sample": f"{rows // 2} middle rows, {cpu_s:.1f}s"},
+                          "gpu_vs_cpu": gpu / cpu}
+        v = case_view("c3", None, aa=False)
+        rc = v.rect()
+        W, H = v.real_width, v.real_height
+        r.render_mp(W, 8, v.depth, rc.xmin, rc.ymax, rc.width, v.precision)   # warm-up
+        t0 = time.perf_counter()
+        _, st = r.render_mp(W, H, v.depth, rc.xmin, rc.ymax, rc.width, v.precision)
+        wall = time.perf_counter() - t0
+        gpu = st["pixel_iters"] / wall
+        rows, cpu_its, cpu_s = 2, 0, 0.0
+        if O.has_mpfr():
+            while cpu_s < args.cpu_seconds / 2 and rows <= H:
+                row0 = H // 2 - rows // 2
+                t0 = time.perf_counter()
+                _, cpu_its = O.render_mpfr(W, H, v.depth, v.precision, rc.xmin, rc.ymax,
+                                           rc.width, row0=row0, nrows=rows, threads=threads)
+                cpu_s = time.perf_counter() - t0
+                rows *= 2
+        cpu = cpu_its / cpu_s if cpu_s else None
+        out["c3_multi_limb"] = {"value": gpu, "unit": "pixel-iters/s", "frame": f"{W}x{H}",
+                                "words": st["words"], "kernel_ms": st["kernel_ms"],
+                                "wall_ms": wall * 1e3,
+                                "cpu_baseline": {"value": cpu, "cores": threads, "kind": "port",
+                                                 "sample": f"{rows // 2} middle rows, MPFR "
+                                                           f"{v.precision}-bit, {cpu_s:.1f}s"},
+                                "gpu_vs_cpu": (gpu / cpu) if cpu else None}
+    return out
 
 
 def run_serving(args, local) -> dict:
@@ -383,6 +452,8 @@ def run_ours(args, view, world, rank, local, dist):
         "perturb_vs_plain": (value / world / plain["value"]) if plain else None,
     }
     r.close()
+    if not args.no_configs:
+        line["plain_configs"] = run_plain_configs(args, local)
     if args.serve_requests > 0:
         line["serving"] = run_serving(args, local)
     if not args.no_cpu_baseline:
