@@ -192,6 +192,28 @@ int mdzgpu_render_mp_noalloc(const mdzgpu_frame* f, const mdzgpu_mpval* xmin,
                              const mdzgpu_mpval* julia_im, int64_t precision,
                              int32_t words, int32_t* d_counts, void* stream);
 
+/* Colouring epilogue (MDZ's palette_apply, src/palette.c:406-463, for
+ * aa = 1; do_anti_aliasing, src/render.c:108-158 with get_pixel_colour,
+ * src/palette.c:466-503, for aa > 1) on the GPU: raw counts [real_h][real_w]
+ * to RGB [real_h/aa][real_w/aa] packed as MDZ packs them (r | g << 8 |
+ * b << 16 on little-endian hosts), identical to the reference's colours for
+ * 0 <= count * colour_scale + offset < 2^31.  With the _device form the
+ * counts never leave the GPU and only the RGB image is copied out. */
+typedef struct mdzgpu_palette {
+    const uint32_t* colours;  /* host array of `indexes` colours (palette[]) */
+    int32_t indexes;          /* pal_indexes, 2..256 */
+    int32_t offset;           /* pal_offset */
+    double colour_scale;      /* img->colour_scale */
+    int32_t interpolate;      /* img->palette_ip */
+    int32_t pad;
+} mdzgpu_palette;
+int mdzgpu_colour(mdzgpu_ctx* ctx, const int32_t* counts, int32_t real_w,
+                  int32_t real_h, int32_t aa, const mdzgpu_palette* pal,
+                  uint32_t* rgb);
+int mdzgpu_colour_device(mdzgpu_ctx* ctx, const int32_t* d_counts,
+                         int32_t real_w, int32_t real_h, int32_t aa,
+                         const mdzgpu_palette* pal, uint32_t* d_rgb);
+
 /* Largest `words` value the MP kernel is built for. */
 int32_t mdzgpu_mp_max_words(void);
 

@@ -109,6 +109,28 @@ class Renderer:
         del keep
         return st.as_dict()
 
+    # -- colouring -------------------------------------------------------------
+    def colour(self, counts: np.ndarray, aa: int, palette, colour_scale: float = 1.0,
+               interpolate: bool = False, offset: int = 0) -> np.ndarray:
+        """MDZ's colouring on the GPU: uint32 [H/aa][W/aa], r | g << 8 | b << 16."""
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        H, W = counts.shape
+        pal_arr = np.ascontiguousarray(palette, dtype=np.uint32)
+        pal = native.Palette(pal_arr.ctypes.data, len(pal_arr), offset, colour_scale,
+                             int(interpolate), 0)
+        out = np.empty((H // aa, W // aa), np.uint32)
+        _check(self.lib.mdzgpu_colour(self.ctx, _ptr(counts), W, H, aa, C.byref(pal),
+                                      _ptr(out)))
+        return out
+
+    def colour_device(self, d_counts: int, W: int, H: int, aa: int, palette, d_rgb: int,
+                      colour_scale: float = 1.0, interpolate: bool = False, offset: int = 0):
+        pal_arr = np.ascontiguousarray(palette, dtype=np.uint32)
+        pal = native.Palette(pal_arr.ctypes.data, len(pal_arr), offset, colour_scale,
+                             int(interpolate), 0)
+        _check(self.lib.mdzgpu_colour_device(self.ctx, C.c_void_p(d_counts), W, H, aa,
+                                             C.byref(pal), C.c_void_p(d_rgb)))
+
     # -- perturbation ---------------------------------------------------------
     def render_perturb(self, W: int, H: int, depth: int, cx: MpVal, cy: MpVal, width: MpVal,
                        precision: int, limbs: int = 0, want_mag: bool = False,

@@ -237,6 +237,7 @@ void mdzgpu_destroy(mdzgpu_ctx* ctx)
     ctx->lists.release();
     ctx->pinned.release();
     ctx->staging.release();
+    ctx->palette.release();
     ctx->pstate.release();
     ctx->pqueue.release();
     ctx->stepinfo.release();

@@ -72,6 +72,7 @@ struct mdzgpu_ctx {
     mdz::DevBuf pstate;     // perturbation pixel state between steps (32 B/pixel)
     mdz::DevBuf pqueue;     // step counters + two pixel queues
     mdz::PinnedBuf stepinfo;  // step results read by the host
+    mdz::DevBuf palette;    // colouring: up to 256 colours
 };
 
 namespace mdz {
@@ -186,6 +187,11 @@ int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in,
                         cudaEvent_t after = nullptr);
 // Orbit + FP32 pixel pass in one cooperative launch (progress words in p).
 int launch_fused(mdzgpu_ctx* ctx, const OrbitLaunch& o, const PerturbLaunch& p, cudaStream_t s);
+
+// Colouring epilogue over device counts (palette already on the device).
+int launch_colour(mdzgpu_ctx* ctx, const int32_t* d_raw, int real_w, int real_h, int aa,
+                  const mdzgpu_palette* pal, const uint32_t* d_palette, uint32_t* d_rgb,
+                  cudaStream_t s);
 
 // Fixed-point conversion helpers (host).  A fixed-point number has `words`
 // 32-bit words, two's complement, least significant first, and

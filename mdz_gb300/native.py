@@ -40,6 +40,11 @@ class MpValStruct(C.Structure):
                 ("d", C.POINTER(C.c_uint64))]
 
 
+class Palette(C.Structure):
+    _fields_ = [("colours", C.c_void_p), ("indexes", C.c_int32), ("offset", C.c_int32),
+                ("colour_scale", C.c_double), ("interpolate", C.c_int32), ("pad", C.c_int32)]
+
+
 class ServeConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_requests", C.c_int32),
                 ("arena_bytes", C.c_int64), ("staging_bytes", C.c_int64),
@@ -104,6 +109,9 @@ _SIGS = {
                                          C.c_int64, C.c_int32, C.c_int64, P, P, P, P,
                                          C.POINTER(C.c_int64)]),
     "mdzgpu_mp_max_words": (C.c_int32, []),
+    "mdzgpu_colour": (C.c_int, [P, P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(Palette), P]),
+    "mdzgpu_colour_device": (C.c_int, [P, P, C.c_int32, C.c_int32, C.c_int32,
+                                       C.POINTER(Palette), P]),
     "mdzgpu_fx_from_mpval": (C.c_int, [C.POINTER(MpValStruct), C.c_int32, P]),
     "mdzgpu_render_mp_noalloc": (C.c_int, [C.POINTER(Frame)] + [C.POINTER(MpValStruct)] * 5
                                  + [C.c_int64, C.c_int32, P, P]),

@@ -47,13 +47,18 @@ class Rect:
 
 
 def mdz_rect(user_w: int, user_h: int, precision: int, cx: str | Fraction,
-             cy: str | Fraction, size: str | Fraction) -> Rect:
-    """xmin, xmax, ymax, width of image_info after render.c:34-35."""
+             cy: str | Fraction, size: str | Fraction, input_prec: int | None = None) -> Rect:
+    """xmin, xmax, ymax, width of image_info after render.c:34-35.  cx, cy,
+    size are first rounded to `input_prec` bits (default: the view's
+    precision, as mpfr_set_str into a p-bit variable does); values that
+    already sit in the coords struct (e.g. a centre computed from a
+    rectangle) pass input_prec = coords_precision(precision)."""
     P = coords_precision(precision)
     Pi = img_precision(precision)
-    cxv = _r(parse_number(cx) if isinstance(cx, str) else Fraction(cx), precision)
-    cyv = _r(parse_number(cy) if isinstance(cy, str) else Fraction(cy), precision)
-    sz = _r(parse_number(size) if isinstance(size, str) else Fraction(size), precision)
+    ip = precision if input_prec is None else input_prec
+    cxv = _r(parse_number(cx) if isinstance(cx, str) else Fraction(cx), ip)
+    cyv = _r(parse_number(cy) if isinstance(cy, str) else Fraction(cy), ip)
+    sz = _r(parse_number(size) if isinstance(size, str) else Fraction(size), ip)
     aspect = Fraction(user_w / user_h)  # a double, exactly
     if aspect > 1:
         width = _r(sz, P)
@@ -106,7 +111,8 @@ class View:
         return self.height * self.aa
 
     def rect(self) -> Rect:
-        return mdz_rect(self.width, self.height, self.precision, self.cx, self.cy, self.size)
+        return mdz_rect(self.width, self.height, self.precision, self.cx, self.cy, self.size,
+                        self.extra.get("coords_input_prec"))
 
     def julia(self) -> tuple[MpVal, MpVal]:
         """u.julia.c_re / c_im as image_info holds them: c_re at max(p, 80)

@@ -41,4 +41,11 @@ gcc $COMMON -mlong-double-64 -ffp-contract=off -DMDZ_SHIM_LD_AS_D \
     $SRCS "$HERE/ref_driver.c" -o "$OUT/libmdzref_d.so" "$MPFR" "$GMP" -lm -lpthread
 gcc $COMMON -ffp-contract=off \
     $SRCS "$HERE/ref_driver.c" -o "$OUT/libmdzref_ld.so" "$MPFR" "$GMP" -lm -lpthread
-echo "build_ref: built $OUT/libmdzref_d.so $OUT/libmdzref_ld.so"
+# colouring (palette.c, render.c) and the .mdz settings loader (image_info.c,
+# mdzfileio.c, setting.c) on top of the hot path, driven by ref_io_driver.c
+IOFILES="palette.c render.c image_info.c mdzfileio.c setting.c globals.c cmdline.c"
+IOSRCS="$SRCS"
+for f in $IOFILES; do IOSRCS="$IOSRCS $SRC/$f"; done
+gcc $COMMON -include limits.h -ffp-contract=off \
+    $IOSRCS "$HERE/ref_io_driver.c" -o "$OUT/libmdzref_io.so" "$MPFR" "$GMP" -lm -lpthread
+echo "build_ref: built $OUT/libmdzref_d.so $OUT/libmdzref_ld.so $OUT/libmdzref_io.so"

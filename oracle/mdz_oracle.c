@@ -28,6 +28,88 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* ---- colouring (TEST INFRASTRUCTURE restatement) ----
+ * palette_apply (src/palette.c:406-463) for aa = 1 and do_anti_aliasing
+ * (src/render.c:108-158) through get_pixel_colour (src/palette.c:466-503)
+ * for aa > 1, on raw counts `raw` [real_h][real_w] into rgb [user_h][user_w].
+ * Colours use MDZ's little-endian packing r | g << 8 | b << 16.  Doubles are
+ * formed exactly as the C code forms them (this file is built without FMA
+ * contraction).  Defined for 0 <= raw * scale + offset < 2^31. */
+#define MDZO_RED(x) ((x) & 0xffu)
+#define MDZO_GREEN(x) (((x) & 0xff00u) >> 8)
+#define MDZO_BLUE(x) (((x) & 0xff0000u) >> 16)
+#define MDZO_RGB(r, g, b) ((uint32_t)(r) | ((uint32_t)(g) << 8) | ((uint32_t)(b) << 16))
+
+static uint32_t colour_of(double val, int ip, const uint32_t* pal, int n, int off)
+{
+    if (val)
+        val += off;
+    if (ip) {
+        const double cval = ceil(val);
+        const double diff = cval - val;
+        const double rdiff = 1.0 - diff;
+        const uint32_t i1 = ((uint32_t)floor(val)) % (uint32_t)(n - 1);
+        const uint32_t i2 = (uint32_t)cval % (uint32_t)(n - 1);
+        const uint32_t c1 = pal[i1], c2 = pal[i2];
+        const uint8_t r = (uint8_t)(diff * MDZO_RED(c1) + rdiff * MDZO_RED(c2));
+        const uint8_t g = (uint8_t)(diff * MDZO_GREEN(c1) + rdiff * MDZO_GREEN(c2));
+        const uint8_t b = (uint8_t)(diff * MDZO_BLUE(c1) + rdiff * MDZO_BLUE(c2));
+        return MDZO_RGB(r, g, b);
+    }
+    if (val == 0)
+        return 0;
+    return pal[(uint32_t)val % (uint32_t)(n - 1)];
+}
+
+int mdzo_colour(const int32_t* raw, int real_w, int real_h, int aa, int ip, double sc,
+                const uint32_t* pal, int n, int off, uint32_t* rgb)
+{
+    if (aa < 1 || real_w % aa || real_h % aa || n < 2 || n > 256)
+        return 0;
+    const int uw = real_w / aa, uh = real_h / aa;
+    for (int y = 0; y < uh; ++y) {
+        for (int x = 0; x < uw; ++x) {
+            if (aa == 1) {
+                const int v = raw[(size_t)y * real_w + x];
+                uint32_t out = 0;
+                if (v) {
+                    const double ip_val = v * sc + off;
+                    if (ip) {
+                        const int ip_cval = (int)ceil(ip_val);
+                        const double ip_diff = ip_cval - ip_val;
+                        const double ip_rdiff = 1.0 - ip_diff;
+                        const int i1 = (int)floor(ip_val) % (n - 1);
+                        const int i2 = ip_cval % (n - 1);
+                        const uint32_t c1 = pal[i1], c2 = pal[i2];
+                        const uint8_t r = (uint8_t)(ip_diff * MDZO_RED(c1) + ip_rdiff * MDZO_RED(c2));
+                        const uint8_t g =
+                            (uint8_t)(ip_diff * MDZO_GREEN(c1) + ip_rdiff * MDZO_GREEN(c2));
+                        const uint8_t b =
+                            (uint8_t)(ip_diff * MDZO_BLUE(c1) + ip_rdiff * MDZO_BLUE(c2));
+                        out = MDZO_RGB(r, g, b);
+                    } else {
+                        out = pal[(uint32_t)ip_val % (uint32_t)(n - 1)];
+                    }
+                }
+                rgb[(size_t)y * uw + x] = out;
+            } else {
+                uint32_t r = 0, g = 0, b = 0;
+                for (int yi = y * aa; yi < y * aa + aa; ++yi)
+                    for (int xi = x * aa; xi < x * aa + aa; ++xi) {
+                        const uint32_t c =
+                            colour_of(raw[(size_t)yi * real_w + xi] * sc, ip, pal, n, off);
+                        r += MDZO_RED(c);
+                        g += MDZO_GREEN(c);
+                        b += MDZO_BLUE(c);
+                    }
+                const uint32_t a2 = (uint32_t)(aa * aa);
+                rgb[(size_t)y * uw + x] = MDZO_RGB(r / a2, g / a2, b / a2);
+            }
+        }
+    }
+    return 1;
+}
+
 #ifdef MDZO_WITH_MPFR
 #include "mpfr.h"
 #endif

@@ -37,6 +37,9 @@ def lib() -> C.CDLL:
             [C.c_double] * 5 + [C.c_int, C.c_void_p]
         L.mdzo_point_fp64.restype = C.c_int64
         L.mdzo_point_fp64.argtypes = [C.c_int, C.c_int64, C.c_double, C.c_double]
+        L.mdzo_colour.restype = C.c_int
+        L.mdzo_colour.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                  C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.mdzo_has_mpfr.restype = C.c_int
         if L.mdzo_has_mpfr():
             L.mdzo_render_mpfr.restype = C.c_int64
@@ -89,6 +92,19 @@ def render_mpfr(W, H, depth, prec, xmin, ymax, width, family=0, fractal=0, julia
     its = lib().mdzo_render_mpfr(W, H, row0, nrows, depth, family, fractal, prec, *args,
                                  threads, out.ctypes.data)
     return out, int(its)
+
+
+def colour(raw: np.ndarray, aa: int, interpolate: bool, scale: float, palette, offset: int = 0):
+    """MDZ's colouring of raw counts (palette_apply for aa = 1,
+    do_anti_aliasing for aa > 1): uint32 [H/aa][W/aa], r | g << 8 | b << 16."""
+    raw = np.ascontiguousarray(raw, dtype=np.int32)
+    H, W = raw.shape
+    pal = np.ascontiguousarray(palette, dtype=np.uint32)
+    out = np.zeros((H // aa, W // aa), np.uint32)
+    if not lib().mdzo_colour(raw.ctypes.data, W, H, aa, int(interpolate), float(scale),
+                             pal.ctypes.data, len(pal), offset, out.ctypes.data):
+        raise ValueError("bad colouring arguments")
+    return out
 
 
 def points_mpfr(cre: list[str], cim: list[str], depth: int, prec: int, fractal=0, threads=1):

@@ -92,6 +92,11 @@ char* mpfr_get_str(char*, mpfr_exp_t*, int, size_t, mpfr_srcptr, mpfr_rnd_t);
 void mpfr_free_str(char*);
 void mpfr_free_cache(void);
 int mpfr_printf(const char*, ...);
+/* the stream functions are exported under these names (they take a FILE*) */
+#define mpfr_out_str __gmpfr_out_str
+#define mpfr_fprintf __gmpfr_fprintf
+size_t __gmpfr_out_str(FILE*, int, size_t, mpfr_srcptr, mpfr_rnd_t);
+int __gmpfr_fprintf(FILE*, const char*, ...);
 int mpfr_snprintf(char*, size_t, const char*, ...);
 const char* mpfr_get_version(void);
 

@@ -7,6 +7,7 @@ the reference sources exist; the GPU machine only reads the outputs).
   python tests/golden/make_golden.py perturb   # perturb_c4.npz (MPFR at 2176 bits)
   python tests/golden/make_golden.py abi       # abi_layout.json (reference struct offsets)
   python tests/golden/make_golden.py centres   # serve_centres.json (serving stream centres)
+  python tests/golden/make_golden.py colour    # colour.npz (reference palette_apply / AA)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -205,6 +206,50 @@ def make_centres() -> None:
                                        cy=hexfloat(bim)))
             print("centre", fractal, seed, f"{time.time() - t0:.1f}s", flush=True)
             (GOLD / "serve_centres.json").write_text(json.dumps(out, indent=1))
+
+
+# Colouring fixtures: the reference's own palette_apply / do_anti_aliasing
+# (oracle/_ref/libmdzref_io.so) on seeded counts, palettes and settings,
+# including the palettes and colour settings of the gallery files.
+def make_colour() -> None:
+    import ctypes as C
+    lib = C.CDLL(str(ROOT / "oracle" / "_ref" / "libmdzref_io.so"))
+    from mdz_gb300.mdzfile import load as load_mdz
+    rng = np.random.Generator(np.random.PCG64(2024))
+    cases = []
+    for f in sorted(GALLERY.glob("*.mdz")):
+        try:
+            s = load_mdz(f)
+        except Exception:
+            continue
+        cases.append(dict(palette=s.palette, scale=s.colour_scale, ip=int(s.palette_ip),
+                          offset=s.palette_offset, tag=f.stem))
+    for k in range(12):
+        n = int(rng.integers(2, 257))
+        cases.append(dict(palette=[int(x) for x in rng.integers(0, 2 ** 24, n)],
+                          scale=float(rng.choice([1.0, 0.25, 0.37, 2.5, 7.125])),
+                          ip=int(k % 2), offset=int(rng.integers(0, 256)), tag=f"random{k}"))
+    arrays, meta = {}, []
+    for i, c in enumerate(cases):
+        for aa in (1, 2, 3):
+            H, W = 6 * aa, 10 * aa
+            raw = rng.integers(0, 5000, (H, W)).astype(np.int32)
+            raw[rng.random((H, W)) < 0.15] = 0
+            pal = np.asarray(c["palette"], np.uint32)
+            out = np.zeros((H // aa, W // aa), np.uint32)
+            ok = lib.mdzref_io_colour(raw.ctypes.data_as(C.c_void_p), W, H, aa, c["ip"],
+                                      C.c_double(c["scale"]), pal.ctypes.data_as(C.c_void_p),
+                                      len(pal), c["offset"], out.ctypes.data_as(C.c_void_p))
+            assert ok
+            key = f"c{i}_aa{aa}"
+            arrays[key + "_raw"] = raw
+            arrays[key + "_pal"] = pal
+            arrays[key + "_rgb"] = out
+            meta.append(dict(key=key, aa=aa, ip=c["ip"], scale=c["scale"], offset=c["offset"],
+                             tag=c["tag"]))
+    np.savez_compressed(GOLD / "colour.npz", **arrays)
+    (GOLD / "colour.json").write_text(json.dumps(meta, indent=1))
+    print("colour cases", len(meta))
 
 
 # --------------------------------------------------------------------------
@@ -462,7 +507,7 @@ def main(argv: list[str]) -> None:
     what = argv[1:] or ["fp64"]
     for w in what:
         {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
-         "perturb": make_perturb, "centres": make_centres}[w]()
+         "perturb": make_perturb, "centres": make_centres, "colour": make_colour}[w]()
 
 
 if __name__ == "__main__":
