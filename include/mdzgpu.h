@@ -218,7 +218,10 @@ int mdzgpu_colour_device(mdzgpu_ctx* ctx, const int32_t* d_counts,
 int32_t mdzgpu_mp_max_words(void);
 
 /* Perturbation path (new method; the reference has none).  Renders the
- * Mandelbrot family/formula around the centre (cx, cy) with real-axis
+ * Mandelbrot family with the Mandelbrot, burning ship or generalized celtic
+ * formula (f->fractal; the folded formulas take |c + d| - |c| from the
+ * orbit's exact side of the fold, and an exact FP64 step wherever a pixel
+ * can cross it) around the centre (cx, cy) with real-axis
  * `width`: pixel (ix, line) is c = (cx + (2 ix - W) hs, cy + (H - 2 line) hs)
  * where hs = width / (2 W) rounded to 40 significant bits (exactly the value
  * mdzgpu_perturb_spacing returns; this is MDZ's centre/size geometry,
@@ -254,6 +257,15 @@ int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx,
                            int32_t limbs, int64_t max_k, double* z_re,
                            double* z_im, double* d_mant, int32_t* d_exp,
                            int64_t* len);
+
+/* The same for the burning ship (Im' = 2 |Re Im| + Ci) and generalized
+ * celtic (Re' = |Re^2 - Im^2| + Cr) formulas (`fractal` = MDZ_BURNING_SHIP /
+ * MDZ_GENERALIZED_CELTIC; MDZ_MANDELBROT as above). */
+int mdzgpu_reference_orbit_formula(mdzgpu_ctx* ctx, int32_t fractal,
+                                   const mdzgpu_mpval* cx, const mdzgpu_mpval* cy,
+                                   int64_t precision, int32_t limbs, int64_t max_k,
+                                   double* z_re, double* z_im, double* d_mant,
+                                   int32_t* d_exp, int64_t* len);
 
 /* Orbit digits chosen for a precision (ceil(precision / 28) + 1, >= 5). */
 int32_t mdzgpu_perturb_limbs(int64_t precision);

@@ -557,7 +557,8 @@ namespace mdz {
 OrbitLayout orbit_layout(size_t entries, int L)
 {
     // zq[entries] float4 | zd[entries] double2 | ze[entries] int |
-    // dd[entries] double | de[entries] int | tiny bits | len + progress words |
+    // dd[entries] double | de[entries] int | tiny bits | fm[entries] double |
+    // fe[entries] int | axis bits | len + progress words |
     // centre digits | rebases | digits[entries][2][L] int (raw orbit, scratch)
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     OrbitLayout o;
@@ -566,7 +567,10 @@ OrbitLayout orbit_layout(size_t entries, int L)
     o.dd = o.ze + al(entries * sizeof(int));
     o.de = o.dd + al(entries * sizeof(double));
     o.tiny = o.de + al(entries * sizeof(int));
-    o.len = o.tiny + al((entries / 32 + 40) * sizeof(unsigned));  // + whole last batches
+    o.fm = o.tiny + al((entries / 32 + 40) * sizeof(unsigned));  // + whole last batches
+    o.fe = o.fm + al(entries * sizeof(double));
+    o.axis = o.fe + al(entries * sizeof(int));
+    o.len = o.axis + al((entries / 32 + 40) * sizeof(unsigned));
     o.dig = o.len + 256;
     o.reb = o.dig + al(2 * (size_t)L * sizeof(int));
     o.raw = o.reb + 256;
@@ -697,8 +701,9 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     int rc = validate_frame(f);
     if (rc)
         return rc;
-    if (f->family != MDZ_FAMILY_MANDEL || f->fractal != MDZ_MANDELBROT) {
-        set_error("perturbation: only the Mandelbrot family / formula is implemented");
+    if (f->family != MDZ_FAMILY_MANDEL || f->fractal == MDZ_VARIANT) {
+        set_error("perturbation: the Mandelbrot family with the Mandelbrot, burning ship or "
+                  "celtic formula");
         return MDZGPU_ERR_UNSUPPORTED;
     }
     MDZ_CUDA_TRY(cudaSetDevice(ctx->device));
@@ -757,6 +762,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.max_k = (int)f->depth + 1;
     o.out_len = (int*)(ob + off_len);
     o.tiny = (unsigned*)(ob + ol.tiny);
+    o.fractal = f->fractal;
+    o.fm = (double*)(ob + ol.fm);
+    o.fe = (int*)(ob + ol.fe);
+    o.axis = (unsigned*)(ob + ol.axis);
     int64_t h2d_extra = 0;
     cudaEvent_t evo;
     MDZ_CUDA_TRY(cudaEventCreate(&evo));
@@ -775,7 +784,8 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     //     resident first wave is paced by the orbit).
     const char* menv = getenv("MDZGPU_PERTURB");
     const char* fenv = getenv("MDZGPU_FUSED");
-    const bool fused = (fenv && fenv[0] == '1') || (menv && !strcmp(menv, "fused"));
+    const bool fused = ((fenv && fenv[0] == '1') || (menv && !strcmp(menv, "fused")))
+                       && f->fractal == MDZ_MANDELBROT;
     const bool stepped = !fused && !(menv && !strcmp(menv, "frame"));
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
     if (stepped) {
@@ -811,6 +821,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.de = o.de;
     p.orbit_len = o.out_len;
     p.tiny = o.tiny;
+    p.fractal = f->fractal;
+    p.fm = o.fm;
+    p.fe = o.fe;
+    p.axis = o.axis;
     p.out = d_out;
     p.mag = d_mag;
     p.sync = (FrameSync*)ctx->sync.ptr;
@@ -884,7 +898,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         q.row0 = 0;
         q.nrows = f->height;
         q.family = MDZ_FAMILY_MANDEL;
-        q.fractal = MDZ_MANDELBROT;
+        q.fractal = f->fractal;
         q.depth = (uint32_t)f->depth;
         q.words = w;
         q.xs = (const uint32_t*)ctx->coords.ptr;
@@ -947,6 +961,19 @@ int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx, const mdzgpu
                            int64_t precision, int32_t limbs, int64_t max_k, double* z_re,
                            double* z_im, double* d_mant, int32_t* d_exp, int64_t* len)
 {
+    return mdzgpu_reference_orbit_formula(ctx, MDZ_MANDELBROT, cx, cy, precision, limbs, max_k,
+                                          z_re, z_im, d_mant, d_exp, len);
+}
+
+int mdzgpu_reference_orbit_formula(mdzgpu_ctx* ctx, int32_t fractal, const mdzgpu_mpval* cx,
+                                   const mdzgpu_mpval* cy, int64_t precision, int32_t limbs,
+                                   int64_t max_k, double* z_re, double* z_im, double* d_mant,
+                                   int32_t* d_exp, int64_t* len)
+{
+    if (fractal < MDZ_MANDELBROT || fractal > MDZ_GENERALIZED_CELTIC) {
+        set_error("reference orbit: formula %d has no multi-limb orbit", fractal);
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
     if (!ctx || max_k < 1 || max_k > 0x7ffffffeLL) {
         set_error("reference orbit: bad arguments");
         return MDZGPU_ERR_ARG;
@@ -990,6 +1017,7 @@ int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx, const mdzgpu
     o.digits = (int*)(ob + off_raw);
     o.max_k = (int)max_k;
     o.out_len = (int*)(ob + off_len);
+    o.fractal = fractal;
     if ((rc = launch_orbit(o, ctx->stream)))
         return rc;
     int n = 0;

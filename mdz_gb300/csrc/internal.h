@@ -53,6 +53,32 @@ struct FrameSync {
 
 }  // namespace mdz
 
+namespace mdz {
+// Completion of a launch without a stream command behind it (a command
+// queued behind a long kernel holds its hardware queue, and the streams
+// that share that queue, until the kernel ends): every thread counts
+// itself out, the last one stores `value` into a pinned host word that the
+// host polls.  `count` is zeroed before the launch.
+struct DoneSignal {
+    unsigned* count = nullptr;
+    volatile int* host = nullptr;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ void done_signal(const DoneSignal& s, int value)
+{
+    if (!s.count)
+        return;
+    __threadfence();
+    const unsigned total = gridDim.x * gridDim.y * gridDim.z * blockDim.x * blockDim.y * blockDim.z;
+    if (atomicAdd(s.count, 1u) + 1u == total) {
+        __threadfence_system();
+        *s.host = value;
+        __threadfence_system();
+    }
+}
+#endif
+}  // namespace mdz
+
 struct mdzgpu_ctx {
     int device = 0;
     int num_sms = 0;
@@ -109,6 +135,10 @@ struct MpLaunch {
     const unsigned* list = nullptr;
     const unsigned* list_count = nullptr;
     float* mag = nullptr;   // |z|^2 at escape (FP32), when non-null
+    DoneSignal done;        // optional: stores 1 when the launch is complete
+                            // (3 when it also reached the list's end)
+    // list pass in chunks: this launch takes tiles tile_base + [0, tile_limit)
+    unsigned tile_base = 0, tile_limit = 0xffffffffu;
 };
 int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
 bool mp_words_supported(int words);
@@ -117,6 +147,14 @@ bool mp_words_supported(int words);
 #define MDZ_MP_WORDS_LIST(X) X(4) X(6) X(8) X(10) X(12) X(16) X(20) X(24) X(28) X(34) X(36)
 template <int N>
 int launch_words(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
+template <int N>
+int preload_words();
+// Loads (and sets up) every multi-limb frame kernel / every perturbation
+// pass kernel now: with lazy module loading the first launch of a kernel
+// waits for the work running on the device, which would stall a server
+// that launches an escalation pass while others run.
+int preload_mp_kernels();
+int preload_perturb_kernels();
 
 struct OrbitLaunch {
     int limbs;              // L radix-2^28 signed digits, F = 28 (L - 1)
@@ -133,6 +171,15 @@ struct OrbitLaunch {
     int* sm_busy = nullptr; // serving: producers per SM id (counted while running)
     int sm_words = 0;
     unsigned* tiny = nullptr;  // [max_k / 32 + 2] bit k: |Z_k|^2 < 2^-120 (FP32)
+    // formula: MDZ_MANDELBROT, MDZ_BURNING_SHIP (Im = 2 |Re Im| + Ci) or
+    // MDZ_GENERALIZED_CELTIC (Re = |Re^2 - Im^2| + Cr)
+    int fractal = 0;
+    // burning ship / celtic: the fold quantity F_k (Re Im, or Re^2 - Im^2)
+    // = fm * 2^fe, its sign in zq[k].w, and bit k of `axis` set where F_k is
+    // within 2^-100 of 0 (a pixel's dz can move it across the fold there)
+    double* fm = nullptr;
+    int* fe = nullptr;
+    unsigned* axis = nullptr;
 };
 int launch_orbit(const OrbitLaunch& p, cudaStream_t s);
 int orbit_max_limbs();
@@ -149,6 +196,10 @@ struct PerturbLaunch {
     const int* de;
     const int* orbit_len;   // device: valid orbit entries
     const unsigned* tiny;   // bit mask of tiny |Z_k| (see OrbitLaunch)
+    int fractal = 0;        // MDZ_MANDELBROT / _BURNING_SHIP / _GENERALIZED_CELTIC
+    const double* fm = nullptr;  // fold quantity F_k = fm * 2^fe (see OrbitLaunch)
+    const int* fe = nullptr;
+    const unsigned* axis = nullptr;
     int32_t* out;
     float* mag;             // |z|^2 at escape (may be null)
     FrameSync* sync;
@@ -167,6 +218,10 @@ struct PerturbLaunch {
     int* orbit_done = nullptr;
     int* orbit_error = nullptr;
     int* producer_sm = nullptr;  // SM id + 1 of the orbit producer block
+    DoneSignal done;             // optional: stores 1 when the launch is complete
+                                 // (3 when it also reached the list's end)
+    // list pass in chunks: this launch takes tiles tile_base + [0, tile_limit)
+    unsigned tile_base = 0, tile_limit = 0xffffffffu;
 };
 // pass 0: FP32 frame pass; pass 1: FP64 pass over list_in
 int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass);
@@ -174,7 +229,9 @@ int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int 
 // progress: progress[1] digits written, [2] entries finished (in whole
 // batches of 256), [3] producer done (final length in *o.out_len), [4] a
 // bounded wait gave up, [5] SM id + 1 of the producer while it runs.
-int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s);
+// `done` (optional) stores 1 when the launch is complete, 2 if it gave up.
+int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s,
+                        DoneSignal done = DoneSignal{});
 // One step of the FP32 pass over the queue in[0..n) (in == nullptr: every
 // pixel of the frame, fresh): pixels read the orbit progress in p (fin_len,
 // orbit_done, orbit_len), iterate at most `budget` iterations, and the
@@ -222,7 +279,7 @@ int mpfr_round_to_fixed(const mdzgpu_mpval* v, long p, int words, uint32_t* out)
 // Reference-orbit buffer: byte offsets of its 256-byte aligned pieces for
 // `entries` entries of L digits (zf at 0).
 struct OrbitLayout {
-    size_t zd, ze, dd, de, tiny, len, dig, reb, raw, bytes;
+    size_t zd, ze, dd, de, tiny, fm, fe, axis, len, dig, reb, raw, bytes;
 };
 OrbitLayout orbit_layout(size_t entries, int L);
 // Multi-limb word count of the perturbation's last escalation pass.

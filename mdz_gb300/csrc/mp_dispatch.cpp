@@ -28,10 +28,22 @@ int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
     }
 }
 
-// Class k >= 1 of the serving engine is the k-th word count of the list.
+int preload_mp_kernels()
+{
+    int rc = MDZGPU_OK;
+#define MDZ_CASE(n)              \
+    if (!rc)                     \
+        rc = preload_words<n>();
+    MDZ_MP_WORDS_LIST(MDZ_CASE)
+#undef MDZ_CASE
+    return rc;
+}
+
+// Class kServePerturbClasses + k of the serving engine is the (k+1)-th word
+// count of the list.
 int serve_mp_class_words(int cls)
 {
-    int k = 0;
+    int k = kServePerturbClasses - 1;
 #define MDZ_CASE(n)      \
     if (++k == cls)      \
         return n;

@@ -180,8 +180,11 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
     const unsigned total = p.list ? (list_n + 31u) / 32u : (unsigned)tiles_x * (unsigned)tiles_y;
     for (;;) {
         unsigned tile = 0;
-        if (lane == 0)
-            tile = (p.stop && *p.stop) ? total : atomicAdd(&p.sync->tile_counter, 1u);
+        if (lane == 0) {
+            const unsigned t = (p.stop && *p.stop) ? 0xffffffffu
+                                                    : atomicAdd(&p.sync->tile_counter, 1u);
+            tile = t >= p.tile_limit ? total : p.tile_base + t;
+        }
         tile = __shfl_sync(0xffffffffu, tile, 0);
         if (tile >= total)
             break;
@@ -252,6 +255,8 @@ __global__ void __launch_bounds__(block_threads<N>()) mp_frame_kernel(MpLaunch p
             }
         }
     }
+    if (p.done.count)
+        done_signal(p.done, (unsigned long long)p.tile_base + p.tile_limit >= total ? 3 : 1);
 }
 
 // Serving: one step of the multi-limb method over its mixed work queue
@@ -266,6 +271,7 @@ __global__ void __launch_bounds__(block_threads<N>()) serve_mp_kernel(ServeDev* 
         return;
     const unsigned cur = d->ctl.cur;
     const unsigned n = d->status.qcount[cls][cur];
+    const ServeClassTimer timer(d, cls, cur, n);
     const unsigned* qin = d->queue[cls][cur];
     unsigned* qout = d->queue[cls][cur ^ 1u];
     unsigned* qout_count = &d->status.qcount[cls][cur ^ 1u];
@@ -379,8 +385,11 @@ __global__ void __launch_bounds__(block_threads<N>()) serve_mp_kernel(ServeDev* 
     }
 }
 
+// Attributes and occupancy of one frame kernel, set up once.  The first
+// call also loads the kernel (with lazy module loading, a load waits for
+// the work running on the device, so servers call it before they start).
 template <int N, int FRACTAL, bool JULIA>
-int launch_typed(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
+int typed_blocks_per_sm(int* out)
 {
     constexpr int threads = block_threads<N>();
     const size_t smem = c_in_smem<N>() ? (size_t)2 * N * threads * sizeof(uint32_t) : 0;
@@ -390,11 +399,23 @@ int launch_typed(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
             MDZ_CUDA_TRY(cudaFuncSetAttribute(mp_frame_kernel<N, FRACTAL, JULIA>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem));
+        int b = 0;
         MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &blocks_per_sm, mp_frame_kernel<N, FRACTAL, JULIA>, threads, smem));
-        if (blocks_per_sm < 1)
-            blocks_per_sm = 1;
+            &b, mp_frame_kernel<N, FRACTAL, JULIA>, threads, smem));
+        blocks_per_sm = b < 1 ? 1 : b;
     }
+    *out = blocks_per_sm;
+    return MDZGPU_OK;
+}
+
+template <int N, int FRACTAL, bool JULIA>
+int launch_typed(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
+{
+    constexpr int threads = block_threads<N>();
+    const size_t smem = c_in_smem<N>() ? (size_t)2 * N * threads * sizeof(uint32_t) : 0;
+    int blocks_per_sm = 1;
+    if (int rc = typed_blocks_per_sm<N, FRACTAL, JULIA>(&blocks_per_sm))
+        return rc;
     const long tiles = p.list ? ((long)p.W * p.nrows + 31) / 32
                               : (long)((p.W + kTileW - 1) / kTileW) * ((p.nrows + kTileH - 1) / kTileH);
     long grid = (long)ctx->num_sms * blocks_per_sm;
@@ -452,12 +473,34 @@ int launch_serve_mp_words(ServeDev* d, int mp_class, int num_sms, cudaStream_t s
     return MDZGPU_OK;
 }
 
+template <int N>
+int preload_words()
+{
+    int b = 0, rc = MDZGPU_OK;
+    for (int j = 0; j < 2 && !rc; ++j) {
+        const bool julia = j == 1;
+        rc = julia ? typed_blocks_per_sm<N, MDZ_MANDELBROT, true>(&b)
+                   : typed_blocks_per_sm<N, MDZ_MANDELBROT, false>(&b);
+        if (!rc)
+            rc = julia ? typed_blocks_per_sm<N, MDZ_BURNING_SHIP, true>(&b)
+                       : typed_blocks_per_sm<N, MDZ_BURNING_SHIP, false>(&b);
+        if (!rc)
+            rc = julia ? typed_blocks_per_sm<N, MDZ_GENERALIZED_CELTIC, true>(&b)
+                       : typed_blocks_per_sm<N, MDZ_GENERALIZED_CELTIC, false>(&b);
+        if (!rc)
+            rc = julia ? typed_blocks_per_sm<N, MDZ_VARIANT, true>(&b)
+                       : typed_blocks_per_sm<N, MDZ_VARIANT, false>(&b);
+    }
+    return rc;
+}
+
 #ifdef MDZ_MP_WORDS
 // One translation unit per word count (the build compiles this file once for
 // every count in the list) keeps the large unrolled kernels compiling in
 // parallel.
 template int launch_words<MDZ_MP_WORDS>(mdzgpu_ctx*, const MpLaunch&, cudaStream_t);
 template int launch_serve_mp_words<MDZ_MP_WORDS>(ServeDev*, int, int, cudaStream_t);
+template int preload_words<MDZ_MP_WORDS>();
 #endif
 
 }  // namespace mdz

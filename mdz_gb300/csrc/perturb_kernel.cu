@@ -95,6 +95,24 @@ struct OrbitProgress {
     int* error;     // a bounded wait gave up
 };
 
+// Sign of a radix-2^28 digit vector d[0..L) whose digits are bounded well
+// below 2^27 + 2^6 (the top nonzero digit decides); computed by one warp.
+__device__ __forceinline__ int digits_sign_warp(const int2* z, int L, bool imag)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int s = 2; s >= 0; --s) {
+        const int j = lane + 32 * s;
+        const int d = j < L ? (imag ? z[j].y : z[j].x) : 0;
+        const unsigned m = __ballot_sync(0xffffffffu, d != 0);
+        if (m) {
+            const int dt = __shfl_sync(0xffffffffu, d, 31 - __clz(m));
+            return dt > 0 ? 1 : -1;
+        }
+    }
+    return 0;
+}
+
 // The producer, run by kOrbitThreads = 128 threads (threadIdx.x < 128) with
 // named barrier 1: warp w computes part w & 1 (0: Re, 1: Im) over half
 // w >> 1 of every column's terms; the second halves' partial sums meet the
@@ -124,6 +142,8 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
     const int ctop = 2 * L - 2;    // highest column
     const int nslots = (ctop - cbase + 32) / 32;
     const int* cpart = cc[part];
+    const bool ship = p.fractal == MDZ_BURNING_SHIP;
+    const bool celtic = p.fractal == MDZ_GENERALIZED_CELTIC;
     int k = 1;
     for (;; ++k) {
         if (prog && (k & 31) == 0) {
@@ -143,6 +163,8 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
             if (a * a + b * b > 4.0f || k >= p.max_k)
                 break;
         }
+        // burning ship: Im' = 2 |Re| |Im| + Ci = sign(Re) sign(Im) 2 Re Im + Ci
+        const int sxy = ship ? digits_sign_warp(z, L, false) * digits_sign_warp(z, L, true) : 1;
         long long v[3] = {0, 0, 0};
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
@@ -185,15 +207,16 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
                 }
             }
             long long acc = 2 * ((a0 + a1) + (a2 + a3));
-            if (!half) {
-                if (!(c & 1)) {
-                    const int2 h = z[c >> 1];
-                    acc += part == 0 ? (long long)h.x * h.x - (long long)h.y * h.y
-                                     : 2 * (long long)h.x * h.y;
-                }
-                if (c >= L - 1)
-                    acc += cpart[c - (L - 1)];
+            if (!half && !(c & 1)) {
+                const int2 h = z[c >> 1];
+                acc += part == 0 ? (long long)h.x * h.x - (long long)h.y * h.y
+                                 : 2 * (long long)h.x * h.y;
             }
+            if (part == 1)
+                acc *= sxy;
+            // celtic adds Cr after the fold (below)
+            if (!half && c >= L - 1 && !(celtic && part == 0))
+                acc += cpart[c - (L - 1)];
             v[s] = acc;
         }
         if (half) {
@@ -209,22 +232,50 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
             v[s] += partial[part][s][lane];
         // carry propagation: column c+1 is lane+1 (slot s) or lane 0 of
         // slot s+1; two passes bound every digit by 2^27 + 2^5
+        auto carry2 = [&]() {
 #pragma unroll
-        for (int pass = 0; pass < 2; ++pass) {
-            long long dg[3], cy[3];
+            for (int pass = 0; pass < 2; ++pass) {
+                long long dg[3], cy[3];
 #pragma unroll
-            for (int s = 0; s < 3; ++s)
-                digit_split(v[s], dg[s], cy[s]);
+                for (int s = 0; s < 3; ++s)
+                    digit_split(v[s], dg[s], cy[s]);
+#pragma unroll
+                for (int s = 0; s < 3; ++s) {
+                    if (s >= nslots)
+                        break;
+                    long long in = __shfl_up_sync(0xffffffffu, cy[s], 1);
+                    const long long wrap =
+                        __shfl_sync(0xffffffffu, s > 0 ? cy[s - 1] : 0ll, 31);
+                    if (lane == 0)
+                        in = wrap;
+                    v[s] = dg[s] + in;
+                }
+            }
+        };
+        carry2();
+        if (celtic && part == 0) {
+            // Re' = |Re^2 - Im^2| + Cr: the sign of the carried digits is
+            // that of their most significant nonzero one
+            int sg = 0;
+#pragma unroll
+            for (int s = 2; s >= 0; --s) {
+                const int c = cbase + lane + 32 * s;
+                const bool ok = s < nslots && c <= ctop && v[s] != 0;
+                const unsigned m = __ballot_sync(0xffffffffu, ok);
+                if (m && !sg) {
+                    const long long t = __shfl_sync(0xffffffffu, v[s], 31 - __clz(m));
+                    sg = t > 0 ? 1 : -1;
+                }
+            }
 #pragma unroll
             for (int s = 0; s < 3; ++s) {
-                if (s >= nslots)
-                    break;
-                long long in = __shfl_up_sync(0xffffffffu, cy[s], 1);
-                const long long wrap = __shfl_sync(0xffffffffu, s > 0 ? cy[s - 1] : 0ll, 31);
-                if (lane == 0)
-                    in = wrap;
-                v[s] = dg[s] + in;
+                const int c = cbase + lane + 32 * s;
+                if (sg < 0)
+                    v[s] = -v[s];
+                if (s < nslots && c <= ctop && c >= L - 1)
+                    v[s] += cpart[c - (L - 1)];
             }
+            carry2();
         }
         int* out = p.digits + (size_t)(k + 1) * 2 * L + part * L;
 #pragma unroll
@@ -301,8 +352,49 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
         p.ze[k] = 0;
     }
     const float fx = (float)vr, fy = (float)vi;
+    // burning ship / celtic: the fold quantity F_k and its exact sign
+    float fold_sign = 1.f;
+    if (p.fractal == MDZ_BURNING_SHIP || p.fractal == MDZ_GENERALIZED_CELTIC) {
+        double fmv;
+        int fev;
+        if (p.fractal == MDZ_BURNING_SHIP) {
+            // F = Re Im: the product of the two 53-bit roundings
+            fmv = mr * mi;
+            fev = xr + xi;
+        } else {
+            // F = Re^2 - Im^2 = (|Re| - |Im|)(|Re| + |Im|), the difference
+            // formed exactly on the digits
+            const int sr = mr < 0.0 ? -1 : 1, si = mi < 0.0 ? -1 : 1;
+            int dd[kMaxOrbitLimbs], ss[kMaxOrbitLimbs];
+            long long cd = 0, cs = 0;
+            for (int j = 0; j < L; ++j) {
+                long long d, cy;
+                digit_split(sr * (long long)dr[j] - si * (long long)di[j] + cd, d, cy);
+                dd[j] = (int)d;
+                cd = cy;
+                digit_split(sr * (long long)dr[j] + si * (long long)di[j] + cs, d, cy);
+                ss[j] = (int)d;
+                cs = cy;
+            }
+            // |values| < 8: the last carries stay within the top digit
+            dd[L - 1] += (int)(cd << 28);
+            ss[L - 1] += (int)(cs << 28);
+            double md, ms;
+            int xd, xs;
+            digits_to_double(dd, L, -F, md, xd);
+            digits_to_double(ss, L, -F, ms, xs);
+            fmv = md * ms;
+            fev = xd + xs;
+        }
+        if (fmv < 0.0)
+            fold_sign = -1.f;
+        if (p.fm) {
+            p.fm[k] = fmv;
+            p.fe[k] = fmv == 0.0 ? -100000 : fev;
+        }
+    }
     // |Z_k|^2 exactly as the pixel loop forms |z|^2 when dz vanishes in FP32
-    p.zq[k] = make_float4(fx, fy, fmaf(fx, fx, fy * fy), 0.f);
+    p.zq[k] = make_float4(fx, fy, fmaf(fx, fx, fy * fy), fold_sign);
     const double d_approx = vr * vr + vi * vi - 4.0;
     if (fabs(d_approx) > 9.5367431640625e-7 /* 2^-20 */) {
         p.dd[k] = d_approx;
@@ -342,17 +434,26 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
 }
 
 // Bit k of p.tiny: |Z_k|^2 < 2^-120 in FP32 (the pixel pass takes the full
-// floatexp step there when dz is below the FP32 range).  Written per warp of
-// 32 consecutive entries, so every word has one writer.
+// floatexp step there when dz is below the FP32 range); bit k of p.axis:
+// |F_k| < 2^-99 (burning ship / celtic: a dz of the FP32 range can carry a
+// pixel across the fold there).  Written per warp of 32 consecutive
+// entries, so every word has one writer.
 __device__ __forceinline__ void write_tiny_bits(const OrbitLaunch& p, int k, bool valid)
 {
-    bool tiny = false;
+    bool tiny = false, axis = false;
     if (valid) {
         tiny = p.zq[k].z < 7.5e-37f;
+        if (p.fm)
+            axis = p.fm[k] == 0.0 || p.fe[k] <= -99;
     }
     const unsigned bits = __ballot_sync(0xffffffffu, tiny);
-    if (p.tiny && (threadIdx.x & 31) == 0 && k >= 0)
-        p.tiny[k >> 5] = bits;
+    const unsigned abits = __ballot_sync(0xffffffffu, axis);
+    if ((threadIdx.x & 31) == 0 && k >= 0) {
+        if (p.tiny)
+            p.tiny[k >> 5] = bits;
+        if (p.axis)
+            p.axis[k >> 5] = abits;
+    }
 }
 
 __global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
@@ -432,6 +533,8 @@ struct Mant<float> {
     static constexpr float kTinyZ2 = 7.5e-37f;   // |Z|^2 < 2^-120
     static constexpr float kGlitchZ2 = 8.7e-19f; // |Z|^2 < 2^-60
     static constexpr int kForceSlow = 120;   // dc 2^-e would overflow above
+    static constexpr float kFoldEps = 9.5367431640625e-7f;  // 2^-20: sign margin
+    static constexpr double kEps2x16 = 5.684341886080802e-14;  // 16 (2^-24)^2
     __device__ static float scale(float x, int e) { return ldexpf(x, e); }
     __device__ static float fma_(float a, float b, float c) { return fmaf(a, b, c); }
     __device__ static int exponent_of(float a) { return ((__float_as_int(a) >> 23) & 0xff) - 127; }
@@ -444,6 +547,8 @@ struct Mant<double> {
     static constexpr double kTinyZ2 = 1e-300;
     static constexpr double kGlitchZ2 = 8.7e-19;
     static constexpr int kForceSlow = 1000;
+    static constexpr double kFoldEps = 3.552713678800501e-15;  // 2^-48
+    static constexpr double kEps2x16 = 1.9721522630525295e-31;  // 16 (2^-53)^2
     __device__ static double scale(double x, int e) { return ldexp(x, e); }
     __device__ static double fma_(double a, double b, double c) { return fma(a, b, c); }
     __device__ static int exponent_of(double a) { return ilogb(a); }
@@ -459,6 +564,12 @@ struct PixState {
     bool careful;   // slow_if_tiny || force_slow
     bool slow_if_tiny;
     bool force_slow;
+    // folded formulas: estimate of the absolute error of z accumulated by
+    // the rounding of the deltas, err^2 = ke e2 2^(2e) (see fold_ke)
+    T e2;
+    T ke;
+    T kb;           // 2^18 ke 2^(2e): e2 kb = (2^9 err)^2; 0 when 2^(2e) underflows
+    T sm;           // 2^-5 2^e: the fold margin per unit of |t|
 };
 
 template <class T>
@@ -473,6 +584,8 @@ __device__ __forceinline__ void refresh_scale(PixState<T>& st, T dcm_r, T dcm_i,
     // is the reference point itself and never needs it.
     st.force_slow = (dcm_r != (T)0 || dcm_i != (T)0) && (dce - st.e) > Mant<T>::kForceSlow;
     st.careful = st.slow_if_tiny || st.force_slow;
+    st.kb = st.e >= Mant<T>::kSqExp ? (T)262144 * st.ke * st.s * st.s : (T)0;
+    st.sm = (T)0.03125 * st.s;
 }
 
 // Set t, e from a double pair scaled by 2^E.
@@ -599,6 +712,213 @@ __device__ __forceinline__ void load_z(const PerturbLaunch& p, int m, T& zx, T& 
     }
 }
 
+// Fold sign of entry m (burning ship: sign(Re Im), celtic: sign(Re^2 - Im^2),
+// exact from the orbit digits; +1 at 0).
+__device__ __forceinline__ float fold_sign(const PerturbLaunch& p, int m)
+{
+    return p.zq[m].w;
+}
+
+__device__ __forceinline__ bool axis_bit(const PerturbLaunch& p, int m)
+{
+    return (__ldg(p.axis + (m >> 5)) >> (m & 31)) & 1u;
+}
+
+__device__ __forceinline__ bool four_not_axis(const PerturbLaunch& p, int m)
+{
+    const unsigned lo = __ldg(p.axis + (m >> 5));
+    const unsigned hi = ((unsigned)m & 31u) > 28u ? __ldg(p.axis + (m >> 5) + 1) : 0u;
+    return (__funnelshift_r(lo, hi, (unsigned)m & 31u) & 0xfu) == 0u;
+}
+
+// The current z = Z_m + dz is on the same side of the fold as Z_m, and the
+// T-rounded values say so with a margin (burning ship: both signs of z
+// agree with those of Z_m's product; celtic: |Re z| - |Im z| has the sign of
+// Re Z^2 - Im Z^2).  The margin covers the rounding of z (eps) and the
+// error of dz: `dzm` = 2^-5 |dz|, well above the relative error estimate
+// the pixel loop enforces (2^-8).
+template <class T, int FR>
+__device__ __forceinline__ bool fold_certain(T zr, T zi, T Zx, T Zy, T fs, T dzm)
+{
+    const T eps = (T)Mant<T>::kFoldEps;
+    if (FR == MDZ_BURNING_SHIP) {
+        const bool neg = (zr < (T)0) != (zi < (T)0);
+        return (neg ? (T)-1 : (T)1) == fs && fabs(zr) > fmax(eps * fabs(Zx), dzm)
+               && fabs(zi) > fmax(eps * fabs(Zy), dzm);
+    }
+    const T ar = fabs(zr), ai = fabs(zi);
+    return fs * (ar - ai) > Mant<T>::fma_(eps, ar + ai, dzm + dzm);
+}
+
+// Error estimate of the folded formulas' deltas.  Every step rounds t
+// (inj <= 4 eps |t'|), and the step's Jacobian in t is 2 z (times a
+// reflection where a component is folded), so an error grows by |2 z| a
+// step.  The roundings of different steps are independent, so their
+// amplified errors add in quadrature (probabilistic rounding-error
+// analysis: ~sqrt(n) eps after n steps where the worst case is n eps, which
+// after 10^4 FP32 steps would already be 2^-8):
+//   e2' = 4 |z|^2 e2 + |t'|^2,   err^2 = ke e2 2^(2e),   ke = 16 eps^2 K^2
+// with K = 4 standard deviations.  A pixel is sent to the next pass
+// (lost = 64) when err can change a decision (an escape test, a side of
+// the fold) or, in FP32, when at a 4th iteration the relative error of t
+// is above 2^-8 or the absolute error of z above 2^-12 (fold_checkpoint).
+template <class T>
+__device__ __forceinline__ T fold_ke(const PerturbLaunch&)
+{
+    return (T)(Mant<T>::kEps2x16 * 16.0);
+}
+
+template <class T>
+__device__ __forceinline__ bool fold_err_hopeless(const PixState<T>& st)
+{
+    const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
+    return !(st.ke * st.e2 <= (T)1.52587890625e-05 * dd) || !(st.kb * st.e2 <= (T)0.015625);
+}
+
+// The every-4th-iteration check.  A trajectory whose estimate passed the
+// limits goes to the next pass, except in the FP64 pass of a folded
+// formula: there it is marked `lost_track` and its later decisions are no
+// longer sent to the multi-limb pass, since an error that large means the
+// pixel's orbit is chaotic beyond what any fixed precision resolves (MPFR
+// at the reference's precision and at twice it disagree there); such a
+// pixel keeps its FP64 count, as the reference keeps its own.  (The
+// Mandelbrot map is conformal: there a large estimate comes from rebases,
+// and the multi-limb pass settles the pixel.)  Returns true when the pixel
+// stops here, flagged.
+template <class T, int FR>
+__device__ __forceinline__ bool fold_checkpoint(const PerturbLaunch& p, const PixState<T>& st,
+                                                float& lost, bool& lost_track)
+{
+    if (fold_err_hopeless(st)) {
+        if (sizeof(T) == 4 || FR == MDZ_MANDELBROT)
+            lost = fmaxf(lost, 64.f);
+        else
+            lost_track = true;
+    }
+    return lost > p.lost_limit && p.flag_out != nullptr;
+}
+
+// After a rebase (t, e replaced by Z_m + dz in FP64): the error carries
+// over, plus the rounding of Z_m to FP64.
+template <class T>
+__device__ __forceinline__ void fold_rebase_err(const PerturbLaunch& p, int m, PixState<T>& st,
+                                                int e0)
+{
+    const double2 zd = p.zd[m];
+    const int ze = p.ze[m];
+    const double z2 = zd.x * zd.x + zd.y * zd.y;
+    const double add = ldexp(z2 * 4.930380657631324e-32 / (double)st.ke, 2 * (ze - st.e));
+    st.e2 = (T)(ldexp((double)st.e2, 2 * (e0 - st.e)) + add);   // 2^-104 |Z|^2 above
+}
+
+// |z|^2 > 4 for a folded formula, exactly as escape_exact; `unsure` when
+// |z|^2 - 4 is within the error estimate of z.
+template <class T>
+__device__ bool escape_fold(const PerturbLaunch& p, int m, const PixState<T>& st, bool& unsure)
+{
+    const double2 zd = p.zd[m];
+    const int ze = p.ze[m];
+    const double dd = p.dd[m];
+    const int de = p.de[m];
+    const double t2 = 2.0 * (zd.x * (double)st.tr + zd.y * (double)st.ti);
+    const int e2 = ze + st.e;
+    const double t3 = (double)st.tr * st.tr + (double)st.ti * st.ti;
+    const int e3 = 2 * st.e;
+    const int E = max(max(dexp_of(dd) + de, dexp_of(t2) + e2), dexp_of(t3) + e3);
+    const double v = ldexp(dd, de - E) + ldexp(t2, e2 - E) + ldexp(t3, e3 - E);
+    const double margin = ldexp(v, E);
+    const double err = ldexp(sqrt((double)st.ke * (double)st.e2), st.e);
+    unsure = !(fabs(margin) > err * (4.5 + err));
+    return v > 0.0;
+}
+
+// One exact step of a folded formula in FP64 with exponents (dz below the
+// FP32 range, |Z_m| tiny, or z near the fold): with c = F_m (the fold
+// quantity of Z_m) and d its change, the folded part is
+// |c + d| - |c| = sign(c) d while c + d keeps the sign of c, and
+// -sign(c) (2c + d) when it crosses.  The side of the fold is decided from
+// z = Z_m + dz in FP64; where even that can not decide it the pixel is
+// marked (`lost`) for the multi-limb pass.
+template <class T, int FR>
+__device__ __forceinline__ void fold_step(const PerturbLaunch& p, int m, PixState<T>& st, T dcf_r,
+                                          T dcf_i, double dcm_r, double dcm_i, int dce,
+                                          float& lost)
+{
+    const double2 zd = p.zd[m];
+    const int ze = p.ze[m];
+    const double tr = (double)st.tr, ti = (double)st.ti;
+    // unfolded pieces: a = 2 Z dz (exp ae), b = dz^2 (exp be)
+    const double ar = 2.0 * (zd.x * tr - zd.y * ti), ai = 2.0 * (zd.x * ti + zd.y * tr);
+    const int ae = ze + st.e;
+    const double br = tr * tr - ti * ti, bi = 2.0 * tr * ti;
+    const int be = 2 * st.e;
+    // the fold quantity c = fm 2^fe and its exact sign
+    const double fmv = p.fm[m];
+    const int fev = p.fe[m];
+    const double sc = (double)fold_sign(p, m);
+    // side of the fold after adding dz.  Burning ship: the signs of
+    // x = X + dx and y = Y + dy, each summed at its own exponent (a sign is
+    // sure when the sum is not within FP64 rounding of its larger term).
+    // Celtic: the sign of x^2 - y^2 = c + d, c exact from the digits, d from
+    // the delta terms (sure when c + d is not within rounding of |c| + |d|).
+    // Both tests also want the margin above the error estimate of z
+    // (err = ea 2^e).
+    const double eps = 1.4210854715202004e-14;  // 2^-46
+    const double ea = sqrt((double)st.ke * (double)st.e2);
+    double side;  // sign of the fold quantity of z
+    bool sure;
+    if (FR == MDZ_BURNING_SHIP) {
+        const int Ex = max(dexp_of(zd.x) + ze, dexp_of(tr) + st.e);
+        const int Ey = max(dexp_of(zd.y) + ze, dexp_of(ti) + st.e);
+        const double xr = ldexp(zd.x, ze - Ex) + ldexp(tr, st.e - Ex);
+        const double xi = ldexp(zd.y, ze - Ey) + ldexp(ti, st.e - Ey);
+        side = ((xr < 0.0) != (xi < 0.0)) ? -1.0 : 1.0;
+        sure = fabs(xr) > fmax(eps, ldexp(ea, st.e - Ex))
+               && fabs(xi) > fmax(eps, ldexp(ea, st.e - Ey));
+    } else {
+        const int Es = max(max(dexp_of(fmax(fabs(ar), fabs(ai))) + ae,
+                               dexp_of(fmax(fabs(br), fabs(bi))) + be),
+                           dexp_of(fmv) + fev);
+        const double cs = ldexp(fmv, fev - Es);
+        const double a1 = ldexp(ar, ae - Es), b1 = ldexp(br, be - Es);
+        const double v = cs + (a1 + b1);
+        side = v < 0.0 ? -1.0 : 1.0;
+        // | |x|^2 - |y|^2 | moves by at most 2 sqrt2 |z| err + 2 err^2
+        sure = fabs(v) > eps * (fabs(cs) + fabs(a1) + fabs(b1))
+               && fabs(v) > ldexp(ea, st.e - Es) * (6.0 + ldexp(ea, st.e));
+    }
+    if (!sure)
+        lost += 64.f;  // undecidable here: the next pass redoes it
+    const bool cross = side != sc;
+    // pieces at a common exponent E: the folded component is
+    //   sc * d            (no crossing)   or   -sc * (2c + d)   (crossing)
+    // with d = (a + b) (celtic: real parts; ship: imaginary parts / 2 ... x2)
+    double fr_, fi_;   // folded component terms
+    int E = max(max(dexp_of(fmax(fabs(ar), fabs(ai))) + ae,
+                    dexp_of(fmax(fabs(br), fabs(bi))) + be),
+                dexp_of(fmax(fabs(dcm_r), fabs(dcm_i))) + dce);
+    if (cross && fmv != 0.0)
+        E = max(E, dexp_of(fmv) + fev + 2);
+    double rr, ri;
+    if (FR == MDZ_BURNING_SHIP) {
+        // Re: unfolded; Im: 2 (|c + d| - |c|) with d = Z_re dz_im + dz_re Z_im + dz_re dz_im
+        rr = ldexp(ar, ae - E) + ldexp(br, be - E) + ldexp(dcm_r, dce - E);
+        const double dd2 = ldexp(ai, ae - E) + ldexp(bi, be - E);   // = 2 d
+        fi_ = cross ? -sc * (ldexp(fmv, fev + 2 - E) + dd2) : sc * dd2;
+        ri = fi_ + ldexp(dcm_i, dce - E);
+        (void)fr_;
+    } else {
+        // Re: |c + d| - |c| with d = 2 Re(Z dz) + Re(dz^2); Im: unfolded
+        const double d = ldexp(ar, ae - E) + ldexp(br, be - E);
+        fr_ = cross ? -sc * (ldexp(fmv, fev + 1 - E) + d) : sc * d;
+        rr = fr_ + ldexp(dcm_r, dce - E);
+        ri = ldexp(ai, ae - E) + ldexp(bi, be - E) + ldexp(dcm_i, dce - E);
+        (void)fi_;
+    }
+    set_from_double(st, rr, ri, E);
+    refresh_scale(st, dcf_r, dcf_i, dce);
+}
+
 // Per-block copy of the orbit progress: pixel threads read shared memory;
 // one elected thread at a time refreshes it from global memory, so the
 // hundreds of thousands of waiting threads do not hammer one L2 line (which
@@ -661,9 +981,12 @@ struct PixRun {
 };
 
 template <class T>
-__device__ __forceinline__ void pixel_start(PixRun<T>& r, double dcm_r, double dcm_i, int dce)
+__device__ __forceinline__ void pixel_start(PixRun<T>& r, double dcm_r, double dcm_i, int dce,
+                                            T ke)
 {
     set_from_double(r.st, dcm_r, dcm_i, dce);
+    r.st.ke = ke;
+    r.st.e2 = Mant<T>::fma_(r.st.tr, r.st.tr, r.st.ti * r.st.ti);  // the rounding of dc 2^-e
     refresh_scale(r.st, (T)dcm_r, (T)dcm_i, dce);
     r.m = 1;
     r.wz = 1;
@@ -701,6 +1024,28 @@ __device__ __forceinline__ void fast_step(PixState<T>& st, T Zx, T Zy, T zr, T z
     st.tr = Mant<T>::fma_(Zx, u, Mant<T>::fma_(-Zy, v, Mant<T>::fma_(st.s, a, st.dcr)));
     st.ti = Mant<T>::fma_(Zx, v, Mant<T>::fma_(Zy, u, Mant<T>::fma_(st.s, b, st.dci)));
 #endif
+}
+
+// The FP32 / FP64 step of a folded formula away from its fold: the folded
+// component's change is sign(F_m) times the unfolded one (burning ship:
+// Im = 2 |Re Im| + Ci; celtic: Re = |Re^2 - Im^2| + Cr), the other
+// component is Mandelbrot's.
+template <class T, int FR>
+__device__ __forceinline__ void fold_fast_step(PixState<T>& st, T Zx, T Zy, T fs)
+{
+    const T tr = st.tr, ti = st.ti;
+    const T u = tr + tr, v = ti + ti;
+    const T a = Mant<T>::fma_(tr, tr, -ti * ti);
+    const T b = tr * v;
+    if (FR == MDZ_BURNING_SHIP) {
+        st.tr = Mant<T>::fma_(Zx, u, Mant<T>::fma_(-Zy, v, Mant<T>::fma_(st.s, a, st.dcr)));
+        const T w = Mant<T>::fma_(Zx, v, Mant<T>::fma_(Zy, u, st.s * b));
+        st.ti = Mant<T>::fma_(fs, w, st.dci);
+    } else {
+        const T w = Mant<T>::fma_(Zx, u, Mant<T>::fma_(-Zy, v, st.s * a));
+        st.tr = Mant<T>::fma_(fs, w, st.dcr);
+        st.ti = Mant<T>::fma_(Zx, v, Mant<T>::fma_(Zy, u, Mant<T>::fma_(st.s, b, st.dci)));
+    }
 }
 
 // How a pixel learns which reference-orbit entries it may read:
@@ -744,7 +1089,7 @@ __device__ __forceinline__ OrbitSnap orbit_snapshot(const PerturbLaunch& p)
 // continues on the general path, so the operations are the same whether a
 // pixel runs in blocks or not, and a pixel resumed at any iteration gets
 // bit-identical results.
-template <class T, int MODE>
+template <class T, int MODE, int FR = MDZ_MANDELBROT>
 __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, double dcm_i,
                            int dce, uint32_t wz_last, uint32_t& count, BlockOrbitView* view,
                            OrbitSnap snap = OrbitSnap{0, 0})
@@ -761,11 +1106,25 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
         return 0;  // Z_m not finished yet
     T Zx, Zy;
     load_z<T>(p, m, Zx, Zy);
+    T fs = (T)1;   // fold sign of Z_m (burning ship / celtic)
+    if (FR != MDZ_MANDELBROT)
+        fs = (T)fold_sign(p, m);
     T zr = Mant<T>::fma_(st.s, st.tr, Zx);
     T zi = Mant<T>::fma_(st.s, st.ti, Zy);
     const T band_lo = (T)4 - (T)6.1035156e-5;  // 4 - 2^-14
     const T band_hi = (T)4 + (T)6.1035156e-5;
     T magT = (T)r.mag;
+    // error estimate (see fold_ke), carried by the folded formulas and by
+    // every FP64 pass: it grows by 4 |z|^2 (|z|^2 of the z about to be
+    // stepped) and also covers what rebases cancel.  The FP32 Mandelbrot
+    // pass counts the bits its rebases cancel instead.
+    constexpr bool kTrack = FR != MDZ_MANDELBROT || sizeof(T) == 8;
+    const T grow = (T)4;
+    bool lost_track = false;   // FP64: the estimate passed its limits
+    float lost_sink = 0.f;
+    float& rebase_lost = kTrack ? lost_sink : r.lost;
+    if (kTrack)
+        magT = Mant<T>::fma_(zr, zr, zi * zi);
     const uint32_t last = wz_last < p.depth ? wz_last : p.depth;
     uint32_t wz = r.wz;
     bool blocked = false;
@@ -774,8 +1133,62 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
         // blocks: FP32 (the FP64 pass is the rare escalation path), no
         // slow step among the four (dz below the FP32 range needs one only
         // where Z_m is tiny)
-        if (sizeof(T) == 4 && (wz & 3u) == 1u && wz + 3u <= last && m + 4 < avail
-            && !st.force_slow && (!st.slow_if_tiny || four_not_tiny(p, m))) {
+        if (FR != MDZ_MANDELBROT && sizeof(T) == 4 && (wz & 3u) == 1u && wz + 3u <= last
+            && m + 4 < avail && st.s == (T)0 && !st.force_slow && four_not_axis(p, m)) {
+            // folded formulas at deep zoom: z = Z_m in FP32 and no fold
+            // within reach of dz among these entries, so the fold keeps
+            // Z_m's side; same values as the general step with s = 0
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const T tr = st.tr, ti = st.ti;
+                const T u2 = tr + tr, v2 = ti + ti;
+                const T g = grow * magT;
+                if (FR == MDZ_BURNING_SHIP) {
+                    st.tr = Mant<T>::fma_(Zx, u2, Mant<T>::fma_(-Zy, v2, st.dcr));
+                    st.ti = Mant<T>::fma_(fs, Mant<T>::fma_(Zx, v2, Zy * u2), st.dci);
+                } else {
+                    st.tr = Mant<T>::fma_(fs, Mant<T>::fma_(Zx, u2, -Zy * v2), st.dcr);
+                    st.ti = Mant<T>::fma_(Zx, v2, Mant<T>::fma_(Zy, u2, st.dci));
+                }
+                st.e2 = Mant<T>::fma_(g, st.e2, Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti));
+                ++m;
+                const float4 q = p.zq[m];
+                Zx = (T)q.x;
+                Zy = (T)q.y;
+                magT = (T)q.z;
+                fs = (T)q.w;
+                if (magT > band_lo || magT < (T)Mant<T>::kGlitchZ2) {
+                    attention = true;
+                    break;
+                }
+                ++wz;
+            }
+            // the current z for the fold test of the general step (= Z_m)
+            zr = Mant<T>::fma_(st.s, st.tr, Zx);
+            zi = Mant<T>::fma_(st.s, st.ti, Zy);
+            if (!attention) {
+                const T amax = fmax(fabs(st.tr), fabs(st.ti));
+                if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
+                    const int k = Mant<T>::exponent_of(amax);
+                    const T sc = Mant<T>::scale((T)1, -k);
+                    st.tr *= sc;
+                    st.ti *= sc;
+                    st.e += k;
+                    st.e2 = Mant<T>::scale(st.e2, -2 * k);
+                    refresh_scale(st, dcf_r, dcf_i, dce);
+                    zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                    zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                }
+                if (fold_checkpoint<T, FR>(p, st, r.lost, lost_track)) {
+                    r.mag = (float)magT;
+                    count = 0;
+                    return 1;  // the next pass redoes the pixel
+                }
+                continue;
+            }
+        } else if (FR == MDZ_MANDELBROT && sizeof(T) == 4 && (wz & 3u) == 1u && wz + 3u <= last
+                   && m + 4 < avail && !st.force_slow
+                   && (!st.slow_if_tiny || four_not_tiny(p, m))) {
             // iterations wz .. wz+3, orbit entries m+1 .. m+4 all finished
             if (st.s == (T)0) {
                 // dz below the FP32 range (deep zoom): s t and s t^2 vanish
@@ -845,27 +1258,75 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 }
                 if (m >= K - 1) {
                     // end of the reference orbit: rebase onto Z_0 = 0
-                    rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, r.lost, false);
+                    const int e0 = st.e;
+                    rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, rebase_lost, false);
+                    if (kTrack)
+                        fold_rebase_err<T>(p, m, st, e0);
                     m = 0;
                     Zx = (T)0;
                     Zy = (T)0;
+                    fs = (T)1;
                     zr = Mant<T>::fma_(st.s, st.tr, Zx);
                     zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                    if (kTrack)
+                        magT = Mant<T>::fma_(zr, zr, zi * zi);
                     ++r.rebases;
                 }
             }
-            if (st.careful && (st.force_slow || z_tiny<T>(p, m, Zx, Zy))) {
+            const bool careful = st.careful && (st.force_slow || z_tiny<T>(p, m, Zx, Zy));
+            const T g = kTrack ? grow * magT : (T)0;
+            if (FR != MDZ_MANDELBROT) {
+                // with dz below the T range (s = 0) a fold is out of reach
+                // unless the entry is marked: the same choice as the blocks
+                const bool fast =
+                    !careful && !axis_bit(p, m)
+                    && (st.s == (T)0
+                        || fold_certain<T, FR>(zr, zi, Zx, Zy, fs,
+                                               st.sm * fmax(fabs(st.tr), fabs(st.ti))));
+                if (fast) {
+                    fold_fast_step<T, FR>(st, Zx, Zy, fs);
+                } else {
+                    const int e0 = st.e;
+                    float unsure = 0.f;
+                    fold_step<T, FR>(p, m, st, dcf_r, dcf_i, dcm_r, dcm_i, dce, unsure);
+                    if (!lost_track)
+                        r.lost += unsure;
+                    if (st.e != e0)
+                        st.e2 = Mant<T>::scale(st.e2, 2 * (e0 - st.e));
+                }
+            } else if (careful) {
+                const int e0 = st.e;
                 slow_step<T>(p, m, st, dcf_r, dcf_i, dcm_r, dcm_i, dce);
+                if (kTrack && st.e != e0)
+                    st.e2 = Mant<T>::scale(st.e2, 2 * (e0 - st.e));
             } else {
                 fast_step<T>(st, Zx, Zy, zr, zi);
             }
             ++m;
             load_z<T>(p, m, Zx, Zy);
+            if (FR != MDZ_MANDELBROT)
+                fs = (T)fold_sign(p, m);
             zr = Mant<T>::fma_(st.s, st.tr, Zx);
             zi = Mant<T>::fma_(st.s, st.ti, Zy);
             magT = Mant<T>::fma_(zr, zr, zi * zi);
+            if (kTrack)
+                st.e2 = Mant<T>::fma_(g, st.e2, Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti));
         }
-        if (magT > band_lo) {
+        if (kTrack) {
+            // the band widens to 2^9 err where the error estimate of z is larger
+            const T dv = magT - (T)4;
+            if (dv > -(T)6.1035156e-5 || dv * dv <= st.kb * st.e2) {
+                bool unsure;
+                const bool esc = escape_fold<T>(p, m, st, unsure);
+                if (unsure && !lost_track)
+                    r.lost = fmaxf(r.lost, 64.f);
+                if (esc) {
+                    r.mag = (float)magT;
+                    count = wz;
+                    return 1;
+                }
+            }
+        } else if (magT > band_lo) {
             // within 2^-14 of the bailout the rounded Z_m can not decide it
             if (magT > band_hi || escape_exact<T>(p, m, st)) {
                 r.mag = (float)magT;
@@ -877,12 +1338,18 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
         // |z| tiny), decided exactly in FP64
         const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
         if (Mant<T>::fma_(st.s2x4, dd, -magT) >= (T)0 || magT < (T)Mant<T>::kGlitchZ2) {
-            if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, r.lost, true)) {
+            const int e0 = st.e;
+            if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, rebase_lost, true)) {
+                if (kTrack)
+                    fold_rebase_err<T>(p, m, st, e0);
                 m = 0;
                 Zx = (T)0;
                 Zy = (T)0;
+                fs = (T)1;
                 zr = Mant<T>::fma_(st.s, st.tr, Zx);
                 zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                if (kTrack)
+                    magT = Mant<T>::fma_(zr, zr, zi * zi);
                 ++r.rebases;
                 ++wz;
                 continue;
@@ -898,9 +1365,16 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 st.tr *= sc;
                 st.ti *= sc;
                 st.e += k;
+                if (kTrack)
+                    st.e2 = Mant<T>::scale(st.e2, -2 * k);
                 refresh_scale(st, dcf_r, dcf_i, dce);
                 zr = Mant<T>::fma_(st.s, st.tr, Zx);
                 zi = Mant<T>::fma_(st.s, st.ti, Zy);
+            }
+            if (kTrack && fold_checkpoint<T, FR>(p, st, r.lost, lost_track)) {
+                r.mag = (float)magT;
+                count = 0;
+                return 1;  // the next pass redoes the pixel
             }
         }
         ++wz;
@@ -923,16 +1397,16 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
 // below `avail` are finished; a pixel that needs entry m + 1 waits (bounded)
 // for the finisher, and learns the final length K once the producer is done.
 // A wait that gives up raises the error flag and leaves the count 0.
-template <class T, bool STREAM>
+template <class T, bool STREAM, int FR>
 __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
                                   float& mag_out, unsigned& rebases, float& lost,
                                   BlockOrbitView* view)
 {
     PixRun<T> r;
-    pixel_start(r, dcm_r, dcm_i, dce);
+    pixel_start(r, dcm_r, dcm_i, dce, fold_ke<T>(p));
     uint32_t count = 0;
-    const int done = perturb_run<T, STREAM ? kOrbitWait : kOrbitComplete>(p, r, dcm_r, dcm_i, dce,
-                                                                          p.depth, count, view);
+    const int done = perturb_run<T, STREAM ? kOrbitWait : kOrbitComplete, FR>(
+        p, r, dcm_r, dcm_i, dce, p.depth, count, view);
     mag_out = r.mag;
     rebases += r.rebases;
     lost += r.lost;
@@ -951,7 +1425,7 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 // (FP64) walks the list of pixels the previous pass flagged, in warp-sized
 // chunks.  Each pass appends the pixels it could not finish precisely to
 // p.flag_out; pixel-iterations are counted only for pixels it finalises.
-template <class T, bool WANT_MAG, bool LIST, bool STREAM>
+template <class T, bool WANT_MAG, bool LIST, bool STREAM, int FR>
 __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
 {
     __shared__ BlockOrbitView view;
@@ -971,8 +1445,11 @@ __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
     const unsigned list_n = LIST ? *p.list_in_count : 0u;
     for (;;) {
         unsigned tile = 0;
-        if (lane == 0)
-            tile = (p.stop && *p.stop) ? total : atomicAdd(&p.sync->tile_counter, 1u);
+        if (lane == 0) {
+            const unsigned t = (p.stop && *p.stop) ? 0xffffffffu
+                                                    : atomicAdd(&p.sync->tile_counter, 1u);
+            tile = t >= p.tile_limit ? total : p.tile_base + t;
+        }
         tile = __shfl_sync(0xffffffffu, tile, 0);
         if (tile >= total)
             break;
@@ -999,7 +1476,8 @@ __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
             const double dcm_r = (double)(2 * ix - p.W) * p.hs_m;
             const double dcm_i = (double)(p.H - 2 * line) * p.hs_m;
             float mag = 0.f, lost = 0.f;
-            const uint32_t n = perturb_pixel<T, STREAM>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost, &view);
+            const uint32_t n =
+                perturb_pixel<T, STREAM, FR>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost, &view);
             const size_t o = (size_t)lrow * p.W + ix;
             p.out[o] = (int32_t)n;
             if (WANT_MAG)
@@ -1022,10 +1500,15 @@ __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
     }
 }
 
-template <class T, bool WANT_MAG, bool LIST>
+template <class T, bool WANT_MAG, bool LIST, int FR>
 __global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
 {
-    pixel_tiles<T, WANT_MAG, LIST, false>(p);
+    pixel_tiles<T, WANT_MAG, LIST, false, FR>(p);
+    if (p.done.count) {
+        const unsigned long long total = LIST ? (*p.list_in_count + 31u) / 32u : 0u;
+        done_signal(p.done,
+                    (unsigned long long)p.tile_base + p.tile_limit >= total ? 3 : 1);
+    }
 }
 
 // One cooperative launch: block 0 produces the reference orbit (64
@@ -1064,21 +1547,23 @@ __global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, Pe
     __syncthreads();
     if (s_leave)
         return;
-    pixel_tiles<float, WANT_MAG, false, true>(p);
+    pixel_tiles<float, WANT_MAG, false, true, MDZ_MANDELBROT>(p);
 }
 
 // ---- serving: one step of the FP32 pass over a mixed work queue ----
 
-// 32 bytes of resumable state per pixel (two uint4).
+// 32 bytes of resumable state per pixel (two uint4).  |z|^2 at escape is
+// only read from a finished run, so an unfinished one keeps the error
+// bound of the folded formulas in its place.
 __device__ __forceinline__ void store_run(const PixRun<float>& r, uint4* sp)
 {
     sp[0] = make_uint4(__float_as_uint(r.st.tr), __float_as_uint(r.st.ti), (unsigned)r.st.e,
                        (unsigned)r.m);
-    sp[1] = make_uint4(r.wz, __float_as_uint(r.lost), __float_as_uint(r.mag), r.rebases);
+    sp[1] = make_uint4(r.wz, __float_as_uint(r.lost), __float_as_uint(r.st.e2), r.rebases);
 }
 
 __device__ __forceinline__ void load_run(PixRun<float>& r, const uint4* sp, double dcm_r,
-                                         double dcm_i, int dce)
+                                         double dcm_i, int dce, float ke)
 {
     const uint4 a = sp[0], b = sp[1];
     r.st.tr = __uint_as_float(a.x);
@@ -1087,8 +1572,10 @@ __device__ __forceinline__ void load_run(PixRun<float>& r, const uint4* sp, doub
     r.m = (int)a.w;
     r.wz = b.x;
     r.lost = __uint_as_float(b.y);
-    r.mag = __uint_as_float(b.z);
+    r.st.e2 = __uint_as_float(b.z);
+    r.mag = 0.f;
     r.rebases = b.w;
+    r.st.ke = ke;
     refresh_scale(r.st, (float)dcm_r, (float)dcm_i, dce);
 }
 
@@ -1121,21 +1608,28 @@ __device__ __forceinline__ void retire_pixels(bool done, int slot, unsigned* rem
         atomicSub(remaining + slot, (unsigned)__popc(grp));
 }
 
-__global__ void __launch_bounds__(256, 5) serve_perturb_kernel(ServeDev* __restrict__ d)
+// Folded formulas carry the error estimate: 4 blocks per SM leave them 64
+// registers (5 would spill).
+template <int FR>
+__global__ void __launch_bounds__(256, FR == MDZ_MANDELBROT ? 5 : 4)
+    serve_perturb_kernel(ServeDev* __restrict__ d)
 {
-    if (serve_block_leaves(d, 0))
+    // class = formula: 0 Mandelbrot, 1 burning ship, 2 celtic
+    constexpr int cls = FR;
+    if (serve_block_leaves(d, cls))
         return;
     const unsigned cur = d->ctl.cur;
-    const unsigned n = d->status.qcount[0][cur];
-    const unsigned* qin = d->queue[0][cur];
-    unsigned* qout = d->queue[0][cur ^ 1u];
-    unsigned* qout_count = &d->status.qcount[0][cur ^ 1u];
+    const unsigned n = d->status.qcount[cls][cur];
+    const ServeClassTimer timer(d, cls, cur, n);
+    const unsigned* qin = d->queue[cls][cur];
+    unsigned* qout = d->queue[cls][cur ^ 1u];
+    unsigned* qout_count = &d->status.qcount[cls][cur ^ 1u];
     const unsigned long long cancel = d->ctl.cancel;
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned base = 0;
         if (lane == 0)
-            base = atomicAdd(&d->qpull[0], 32u);
+            base = atomicAdd(&d->qpull[cls], 32u);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n)
             break;
@@ -1158,12 +1652,12 @@ __global__ void __launch_bounds__(256, 5) serve_perturb_kernel(ServeDev* __restr
                 uint4* sp = rq.state + (size_t)pix * 2u;
                 PixRun<float> r;
                 if (e & kEntryFresh)
-                    pixel_start(r, dcm_r, dcm_i, p.hs_e);
+                    pixel_start(r, dcm_r, dcm_i, p.hs_e, fold_ke<float>(p));
                 else
-                    load_run(r, sp, dcm_r, dcm_i, p.hs_e);
+                    load_run(r, sp, dcm_r, dcm_i, p.hs_e, fold_ke<float>(p));
                 const uint32_t last = r.wz + d->ctl.budget[slot] - 1u;
                 uint32_t count = 0;
-                if (perturb_run<float, kOrbitSnapshot>(p, r, dcm_r, dcm_i, p.hs_e, last, count,
+                if (perturb_run<float, kOrbitSnapshot, FR>(p, r, dcm_r, dcm_i, p.hs_e, last, count,
                                                        nullptr, orbit_snapshot(p)) == 1) {
                     p.out[pix] = (int32_t)count;
                     if (p.mag)
@@ -1190,7 +1684,7 @@ __global__ void __launch_bounds__(256, 5) serve_perturb_kernel(ServeDev* __restr
 // cooperatively (both blocks resident at once: the finisher waits, bounded,
 // on the producer's progress).
 __global__ void __launch_bounds__(256) orbit_stream_kernel(OrbitLaunch o, OrbitProgress g,
-                                                           int* producer_sm)
+                                                           int* producer_sm, DoneSignal done)
 {
     if (blockIdx.x == 0) {
         unsigned smid = 0;
@@ -1207,9 +1701,11 @@ __global__ void __launch_bounds__(256) orbit_stream_kernel(OrbitLaunch o, OrbitP
             if (o.sm_busy)
                 atomicSub(o.sm_busy + smid % (unsigned)o.sm_words, 1);
         }
-        return;
+    } else {
+        orbit_finisher(o, g);
     }
-    orbit_finisher(o, g);
+    if (done.count)
+        done_signal(done, *(volatile int*)g.error ? 2 : 1);
 }
 
 // One step of the FP32 pass of one frame over a compacted pixel queue:
@@ -1227,8 +1723,9 @@ struct FrameStep {
     unsigned budget;
 };
 
-template <bool WANT_MAG>
-__global__ void __launch_bounds__(256, 5) perturb_step_kernel(PerturbLaunch p, FrameStep q)
+template <bool WANT_MAG, int FR>
+__global__ void __launch_bounds__(256, FR == MDZ_MANDELBROT ? 5 : 4)
+    perturb_step_kernel(PerturbLaunch p, FrameStep q)
 {
     // leave the orbit producer's SM to it, unless no other block works yet
     // (a working block pulls until the queue is empty)
@@ -1267,12 +1764,12 @@ __global__ void __launch_bounds__(256, 5) perturb_step_kernel(PerturbLaunch p, F
             uint4* sp = q.state + (size_t)pix * 2u;
             PixRun<float> r;
             if (e & kEntryFresh)
-                pixel_start(r, dcm_r, dcm_i, p.hs_e);
+                pixel_start(r, dcm_r, dcm_i, p.hs_e, fold_ke<float>(p));
             else
-                load_run(r, sp, dcm_r, dcm_i, p.hs_e);
+                load_run(r, sp, dcm_r, dcm_i, p.hs_e, fold_ke<float>(p));
             const uint32_t last = r.wz + q.budget - 1u;
             uint32_t count = 0;
-            if (perturb_run<float, kOrbitSnapshot>(p, r, dcm_r, dcm_i, p.hs_e, last, count,
+            if (perturb_run<float, kOrbitSnapshot, FR>(p, r, dcm_r, dcm_i, p.hs_e, last, count,
                                                    nullptr, orbit_snapshot(p)) == 1) {
                 p.out[pix] = (int32_t)count;
                 if (WANT_MAG)
@@ -1328,21 +1825,42 @@ __global__ void serve_step_end_kernel(ServeDev* d)
         d->status.qcount[c][cur] = 0u;
         d->qpull[c] = 0u;
         d->qworkers[c] = 0u;
+        d->status.tk[cur ^ 1u][c][0] = ~0ull;   // the next step's time span
+        d->status.tk[cur ^ 1u][c][1] = 0ull;
     }
+    for (int slot = threadIdx.x; slot < kServeSlots; slot += blockDim.x) {
+        const unsigned* fc = d->req[slot].pl.flag_out_count;
+        d->status.flagged[slot] = fc ? *fc : 0u;
+    }
+    if (threadIdx.x == 0)
+        d->status.tstep[cur][1] = ServeClassTimer::now();
+}
+
+__global__ void serve_step_begin_kernel(ServeDev* d)
+{
+    d->status.tstep[d->ctl.cur][0] = ServeClassTimer::now();
 }
 
 }  // namespace
 
-int launch_serve_perturb(ServeDev* d, int num_sms, cudaStream_t s)
+int launch_serve_perturb(ServeDev* d, int formula, int num_sms, cudaStream_t s)
 {
+    const void* fn = formula == MDZ_BURNING_SHIP         ? (const void*)serve_perturb_kernel<1>
+                     : formula == MDZ_GENERALIZED_CELTIC ? (const void*)serve_perturb_kernel<2>
+                                                         : (const void*)serve_perturb_kernel<0>;
     static int bps = 0;
     if (!bps) {
-        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, serve_perturb_kernel,
-                                                                   256, 0));
+        MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, 256, 0));
         if (bps < 1)
             bps = 1;
     }
-    serve_perturb_kernel<<<(unsigned)(num_sms * bps), 256, 0, s>>>(d);
+    const unsigned grid = (unsigned)(num_sms * bps);
+    if (formula == MDZ_BURNING_SHIP)
+        serve_perturb_kernel<1><<<grid, 256, 0, s>>>(d);
+    else if (formula == MDZ_GENERALIZED_CELTIC)
+        serve_perturb_kernel<2><<<grid, 256, 0, s>>>(d);
+    else
+        serve_perturb_kernel<0><<<grid, 256, 0, s>>>(d);
     MDZ_CUDA_TRY(cudaGetLastError());
     return MDZGPU_OK;
 }
@@ -1364,7 +1882,14 @@ int launch_serve_step_end(ServeDev* d, cudaStream_t s)
     return MDZGPU_OK;
 }
 
-int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s)
+int launch_serve_step_begin(ServeDev* d, cudaStream_t s)
+{
+    serve_step_begin_kernel<<<1, 1, 0, s>>>(d);
+    MDZ_CUDA_TRY(cudaGetLastError());
+    return MDZGPU_OK;
+}
+
+int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s, DoneSignal done)
 {
     if (o.limbs < 5 || o.limbs > kMaxOrbitLimbs) {
         set_error("orbit: %d limbs outside [5, %d]", o.limbs, kMaxOrbitLimbs);
@@ -1373,7 +1898,7 @@ int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s)
     OrbitLaunch oo = o;
     OrbitProgress g{progress + 1, progress + 2, progress + 3, progress + 4};
     int* producer_sm = progress + 5;
-    void* args[] = {&oo, &g, &producer_sm};
+    void* args[] = {&oo, &g, &producer_sm, &done};
     MDZ_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)orbit_stream_kernel, dim3(2), dim3(256),
                                              args, 0, s));
     return MDZGPU_OK;
@@ -1384,10 +1909,16 @@ int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in,
                         cudaStream_t s, cudaEvent_t before, cudaEvent_t after)
 {
     const bool mag = p.mag != nullptr;
-    const void* fn = mag ? (const void*)perturb_step_kernel<true>
-                         : (const void*)perturb_step_kernel<false>;
-    static int bps[2] = {0, 0};
-    int& b = bps[mag ? 1 : 0];
+    const int fr = p.fractal == MDZ_BURNING_SHIP ? 1 : p.fractal == MDZ_GENERALIZED_CELTIC ? 2 : 0;
+    const void* fns[2][3] = {{(const void*)perturb_step_kernel<false, 0>,
+                              (const void*)perturb_step_kernel<false, 1>,
+                              (const void*)perturb_step_kernel<false, 2>},
+                             {(const void*)perturb_step_kernel<true, 0>,
+                              (const void*)perturb_step_kernel<true, 1>,
+                              (const void*)perturb_step_kernel<true, 2>}};
+    const void* fn = fns[mag ? 1 : 0][fr];
+    static int bps[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int& b = bps[mag ? 1 : 0][fr];
     if (!b) {
         MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, 0));
         if (b < 1)
@@ -1404,10 +1935,8 @@ int launch_perturb_step(int num_sms, const PerturbLaunch& p, const unsigned* in,
     FrameStep q{in, n, out, counters + 1, counters, counters + 2, state, budget};
     if (before)
         MDZ_CUDA_TRY(cudaEventRecord(before, s));
-    if (mag)
-        perturb_step_kernel<true><<<(unsigned)grid, 256, 0, s>>>(p, q);
-    else
-        perturb_step_kernel<false><<<(unsigned)grid, 256, 0, s>>>(p, q);
+    void* args[] = {(void*)&p, (void*)&q};
+    MDZ_CUDA_TRY(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(256), args, 0, s));
     MDZ_CUDA_TRY(cudaGetLastError());
     if (after)
         MDZ_CUDA_TRY(cudaEventRecord(after, s));
@@ -1427,25 +1956,87 @@ int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
     return MDZGPU_OK;
 }
 
-template <class T, bool WANT_MAG, bool LIST>
-int launch_pass(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
+template <class T, bool WANT_MAG, bool LIST, int FR>
+int pass_blocks_per_sm(int* out)
 {
     static int bps = 0;
     if (!bps) {
+        int b = 0;
         MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &bps, perturb_kernel<T, WANT_MAG, LIST>, 256, 0));
-        if (bps < 1)
-            bps = 1;
+            &b, perturb_kernel<T, WANT_MAG, LIST, FR>, 256, 0));
+        bps = b < 1 ? 1 : b;
     }
+    *out = bps;
+    return MDZGPU_OK;
+}
+
+template <class T, bool WANT_MAG, bool LIST, int FR>
+int launch_pass_fr(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
+{
+    int bps = 1;
+    if (int rc = pass_blocks_per_sm<T, WANT_MAG, LIST, FR>(&bps))
+        return rc;
     long grid = (long)ctx->num_sms * bps;
     const long blocks_needed = (work_items + 7) / 8;
     if (grid > blocks_needed)
         grid = blocks_needed;
     if (grid < 1)
         grid = 1;
-    perturb_kernel<T, WANT_MAG, LIST><<<(unsigned)grid, 256, 0, s>>>(p);
+    perturb_kernel<T, WANT_MAG, LIST, FR><<<(unsigned)grid, 256, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
     return MDZGPU_OK;
+}
+
+template <class T, bool WANT_MAG, bool LIST>
+int launch_pass(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
+{
+    if (p.fractal == MDZ_BURNING_SHIP)
+        return launch_pass_fr<T, WANT_MAG, LIST, 1>(ctx, p, s, work_items);
+    if (p.fractal == MDZ_GENERALIZED_CELTIC)
+        return launch_pass_fr<T, WANT_MAG, LIST, 2>(ctx, p, s, work_items);
+    return launch_pass_fr<T, WANT_MAG, LIST, 0>(ctx, p, s, work_items);
+}
+
+template <int FR>
+int preload_fr()
+{
+    int b = 0, rc = MDZGPU_OK;
+    if (!rc)
+        rc = pass_blocks_per_sm<float, false, false, FR>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<float, true, false, FR>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<double, false, true, FR>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<double, true, true, FR>(&b);
+    cudaFuncAttributes a;
+    if (!rc && (cudaFuncGetAttributes(&a, perturb_step_kernel<false, FR>) != cudaSuccess
+                || cudaFuncGetAttributes(&a, perturb_step_kernel<true, FR>) != cudaSuccess
+                || cudaFuncGetAttributes(&a, serve_perturb_kernel<FR>) != cudaSuccess))
+        rc = MDZGPU_ERR_CUDA;
+    return rc;
+}
+
+int preload_perturb_kernels()
+{
+    int rc = preload_fr<MDZ_MANDELBROT>();
+    if (!rc)
+        rc = preload_fr<MDZ_BURNING_SHIP>();
+    if (!rc)
+        rc = preload_fr<MDZ_GENERALIZED_CELTIC>();
+    cudaFuncAttributes a;
+    if (!rc && (cudaFuncGetAttributes(&a, orbit_stream_kernel) != cudaSuccess
+                || cudaFuncGetAttributes(&a, orbit_kernel) != cudaSuccess
+                || cudaFuncGetAttributes(&a, orbit_finish_kernel) != cudaSuccess
+                || cudaFuncGetAttributes(&a, frame_step_reset_kernel) != cudaSuccess
+                || cudaFuncGetAttributes(&a, serve_enqueue_kernel) != cudaSuccess
+                || cudaFuncGetAttributes(&a, serve_enqueue_count_kernel) != cudaSuccess
+                || cudaFuncGetAttributes(&a, serve_step_begin_kernel) != cudaSuccess
+                || cudaFuncGetAttributes(&a, serve_step_end_kernel) != cudaSuccess))
+        rc = MDZGPU_ERR_CUDA;
+    if (rc == MDZGPU_ERR_CUDA)
+        set_error("perturbation: loading the kernels failed");
+    return rc;
 }
 
 int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass)

@@ -16,12 +16,14 @@
 namespace mdz {
 
 constexpr int kServeSlots = 64;
-// method classes: 0 = perturbation (FP32 pass), 1.. = multi-limb kernels in
+// method classes: 0 / 1 / 2 = perturbation FP32 pass of the Mandelbrot,
+// burning ship and generalized celtic formulas; 3.. = multi-limb kernels in
 // MDZ_MP_WORDS_LIST order
 #define MDZ_COUNT_ONE(n) +1
 constexpr int kServeMpClasses = 0 MDZ_MP_WORDS_LIST(MDZ_COUNT_ONE);
 #undef MDZ_COUNT_ONE
-constexpr int kServeClasses = 1 + kServeMpClasses;
+constexpr int kServePerturbClasses = 3;
+constexpr int kServeClasses = kServePerturbClasses + kServeMpClasses;
 constexpr unsigned kEntrySlotShift = 26;
 constexpr unsigned kEntryFresh = 1u << 25;
 constexpr unsigned kEntryPixelMask = kEntryFresh - 1u;
@@ -40,6 +42,12 @@ struct ServeCtl {
 struct ServeStatus {
     unsigned qcount[kServeClasses][2];
     unsigned remaining[kServeSlots];  // pixels of the main pass not finished
+    // per class and step parity: first block start, last warp end of the
+    // slice kernel (globaltimer ns; ~0 / 0 when the class had no work);
+    // the host scales its budgets so that each class's kernel takes one step
+    unsigned long long tk[2][kServeClasses][2];
+    unsigned long long tstep[2][2];   // per parity: step begin, step end (ns)
+    unsigned flagged[kServeSlots];    // perturbation: pixels the FP32 pass flagged so far
 };
 
 // Per-slot request description (device copy).
@@ -87,6 +95,32 @@ __device__ __forceinline__ bool serve_block_leaves(ServeDev* d, int cls)
 }
 #endif
 
+#ifdef __CUDACC__
+// Records the slice kernel's time span of this step in status.tk (see
+// ServeStatus): constructed after serve_block_leaves, ends with the thread.
+struct ServeClassTimer {
+    unsigned long long* t;
+    bool on;
+    __device__ static unsigned long long now()
+    {
+        unsigned long long v;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+        return v;
+    }
+    __device__ ServeClassTimer(ServeDev* d, int cls, unsigned cur, unsigned n)
+        : t(d->status.tk[cur][cls]), on(n != 0u)
+    {
+        if (on && threadIdx.x == 0)
+            atomicMin(t, now());
+    }
+    __device__ ~ServeClassTimer()
+    {
+        if (on && (threadIdx.x & 31) == 0)
+            atomicMax(t + 1, now());
+    }
+};
+#endif
+
 __host__ __device__ inline unsigned serve_entry(int slot, bool fresh, unsigned pixel)
 {
     return ((unsigned)slot << kEntrySlotShift) | (fresh ? kEntryFresh : 0u) | pixel;
@@ -96,7 +130,7 @@ __host__ __device__ inline unsigned serve_entry(int slot, bool fresh, unsigned p
 // A block placed on an SM where a reference orbit runs leaves at once, but
 // only when another block of the same launch already works the queue: a
 // working block pulls until the queue is empty, so no entry is left behind.
-int launch_serve_perturb(ServeDev* d, int num_sms, cudaStream_t s);
+int launch_serve_perturb(ServeDev* d, int formula, int num_sms, cudaStream_t s);
 int launch_serve_mp(ServeDev* d, int mp_class, int num_sms, cudaStream_t s);
 template <int N>
 int launch_serve_mp_words(ServeDev* d, int mp_class, int num_sms, cudaStream_t s);
@@ -104,7 +138,9 @@ int launch_serve_mp_words(ServeDev* d, int mp_class, int num_sms, cudaStream_t s
 int launch_serve_enqueue(ServeDev* d, int cls, int q, int slot, unsigned npix, cudaStream_t s);
 // End of a step: queue `cur` is consumed; clear its count and the pull counters.
 int launch_serve_step_end(ServeDev* d, cudaStream_t s);
-// Word count of multi-limb class cls (1 ..), 0 if none.
+// Start of a step: stamps status.tstep[cur][0].
+int launch_serve_step_begin(ServeDev* d, cudaStream_t s);
+// Word count of multi-limb class cls (kServePerturbClasses ..), 0 if none.
 int serve_mp_class_words(int cls);
 // Uint4 words of resumable state per pixel of the multi-limb slice kernel.
 inline unsigned serve_mp_state_stride(int words)

@@ -44,6 +44,8 @@ double wall_ms()
 }
 
 constexpr size_t kAlign = 256;
+constexpr int kEscShare = 4;       // escalation passes use 1 / kEscShare of the SMs
+constexpr unsigned kEscTilesPerSm = 32;  // list tiles (32 pixels) per SM and chunk
 inline size_t al(size_t b)
 {
     return (b + kAlign - 1) & ~(kAlign - 1);
@@ -103,7 +105,10 @@ private:
     std::map<size_t, size_t> free_;
 };
 
-enum Phase { kQueued, kRunning, kFinishing, kEnded };
+// After the main pass: kEscWait (queued for the escalation passes),
+// kEscFp64 / kEscMp (that pass in flight), kCopyWait (result copies wait
+// for the orbit launch to end), kFinishing (copies in flight).
+enum Phase { kQueued, kRunning, kEscWait, kEscFp64, kEscMp, kCopyWait, kFinishing, kEnded };
 
 // Offsets of a request's pieces in its device block and its pinned block.
 struct Layout {
@@ -141,7 +146,9 @@ struct Req {
     int cancel_state = MDZGPU_REQ_CANCELLED;
     double t_submit = 0, t_admit = 0, t_done = 0;
     int64_t pixel_iters = 0, esc_fp64 = 0, esc_mp = 0, rebases = 0, steps = 0;
-    cudaEvent_t ev_orbit = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_done = nullptr;
+    unsigned flagged = 0;        // pixels the FP32 pass sent to the escalation passes
+    unsigned esc_base = 0;       // escalation pass: list tiles launched so far
     bool orbit_running = false;  // streamed orbit not yet complete
     bool cancelled = false;      // finishing only to release the memory
 };
@@ -220,14 +227,16 @@ int prepare(const mdzgpu_request* q, Req& r)
         return MDZGPU_ERR_ARG;
     }
     int method = q->method;
+    // perturbation for the Mandelbrot, burning ship and celtic formulas; the
+    // hybrid (its formula alternates per iteration) on the multi-limb kernel
     if (method == MDZGPU_METHOD_AUTO)
-        method = q->fractal == MDZ_MANDELBROT ? MDZGPU_METHOD_PERTURB : MDZGPU_METHOD_MULTI_LIMB;
+        method = q->fractal == MDZ_VARIANT ? MDZGPU_METHOD_MULTI_LIMB : MDZGPU_METHOD_PERTURB;
     if (method != MDZGPU_METHOD_PERTURB && method != MDZGPU_METHOD_MULTI_LIMB) {
         set_error("serve: unknown method %d", q->method);
         return MDZGPU_ERR_ARG;
     }
-    if (method == MDZGPU_METHOD_PERTURB && q->fractal != MDZ_MANDELBROT) {
-        set_error("serve: perturbation is implemented for the Mandelbrot formula only");
+    if (method == MDZGPU_METHOD_PERTURB && q->fractal == MDZ_VARIANT) {
+        set_error("serve: perturbation is not implemented for the mandel-celtic hybrid");
         return MDZGPU_ERR_UNSUPPORTED;
     }
     if (!q->counts) {
@@ -253,7 +262,7 @@ int prepare(const mdzgpu_request* q, Req& r)
         return MDZGPU_ERR_UNSUPPORTED;
     }
     if (method == MDZGPU_METHOD_PERTURB) {
-        r.cls = 0;
+        r.cls = r.fractal;   // perturbation classes are indexed by formula
         r.limbs = mdzgpu_perturb_limbs(r.precision);
         if (r.limbs < 5 || r.limbs > orbit_max_limbs()) {
             set_error("serve: %d orbit digits outside [5, %d]", r.limbs, orbit_max_limbs());
@@ -268,7 +277,7 @@ int prepare(const mdzgpu_request* q, Req& r)
         }
     } else {
         r.cls = 0;
-        for (int c = 1; c < kServeClasses; ++c)
+        for (int c = kServePerturbClasses; c < kServeClasses; ++c)
             if (serve_mp_class_words(c) == r.words)
                 r.cls = c;
         if (!r.cls) {
@@ -292,7 +301,7 @@ int prepare(const mdzgpu_request* q, Req& r)
 // duration into per-request budgets.
 double class_rate(int cls)
 {
-    if (cls == 0)
+    if (cls < kServePerturbClasses)
         return 3.0e11;
     const double w = (double)serve_mp_class_words(cls);
     return 2.0e9 * (34.0 / w) * (34.0 / w);
@@ -316,6 +325,19 @@ struct Server {
     int device = 0, num_sms = 0;
     cudaStream_t main = nullptr;
     cudaStream_t side[kServeSlots] = {};
+    // low priority: each request's result copies (fin) and the escalation
+    // passes of all requests, one after another (esc), on at most
+    // 1 / kEscShare of the SMs so that the steps keep the rest
+    cudaStream_t fin[kServeSlots] = {};
+    cudaStream_t esc = nullptr;
+    // No stream command is ever queued behind a long kernel (it would hold
+    // a hardware queue shared with other streams, the steps' among them):
+    // the orbit and escalation kernels report their end in pinned host
+    // words, and the host queues what follows them.  One escalation pass
+    // runs at a time.
+    std::deque<std::shared_ptr<Req>> esc_fifo;
+    std::shared_ptr<Req> esc_cur;
+    char* stage_dev = nullptr;  // device alias of stage_host
     cudaStream_t branch[kServeClasses] = {};
     cudaEvent_t fork = nullptr, join[kServeClasses] = {};
     cudaGraph_t graph = nullptr;
@@ -330,6 +352,13 @@ struct Server {
     Arena arena, stage;
     unsigned cur = 0;
     long qhost[kServeClasses] = {};      // entries in queue `cur`
+    // budget feedback: each class's slice kernel should take one step;
+    // rate_adj scales its throughput guess by the time it actually took
+    double rate_adj[kServeClasses];
+    double class_ms[kServeClasses] = {};  // summed slice kernel time
+    double graph_ms = 0, lead_ms = 0;     // device step spans; begin to first slice
+    double loop_ms[9] = {};  // host loop: cancels, admit, orbits, step, finish, idle;
+                             // inside step: before the graph, start_finish, graph launch
     long inflight[kServeClasses] = {};   // admitted pixels per class
     std::shared_ptr<Req> slots[kServeSlots];
     int launches_per_step = 0;
@@ -355,6 +384,17 @@ struct Server {
     void poll_orbits();
     int step();
     int start_finish(const std::shared_ptr<Req>& r);
+    int advance_finishing();
+    int launch_escalation(const std::shared_ptr<Req>& r, bool mp_pass);
+    int enqueue_copies(const std::shared_ptr<Req>& r);
+    volatile int* hflag(const std::shared_ptr<Req>& r, int off)
+    {
+        return (volatile int*)(stage_host + r->host_off + r->lay.h_misc + off);
+    }
+    volatile int* dflag(const std::shared_ptr<Req>& r, int off)
+    {
+        return (volatile int*)(stage_dev + r->host_off + r->lay.h_misc + off);
+    }
     void poll_finishing();
     void end(const std::shared_ptr<Req>& r, int state, int error);
     void check_cancels();
@@ -388,9 +428,14 @@ int Server::init(const mdzgpu_serve_config* c)
     MDZ_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
     int lo = 0, hi = 0;
     MDZ_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    MDZ_CUDA_TRY(cudaStreamCreateWithFlags(&main, cudaStreamNonBlocking));
+    // priorities: orbits (side) highest, the steps (main) above the result
+    // copies and escalation passes (fin, esc), which take what is left
+    MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&main, cudaStreamNonBlocking, (lo + hi) / 2));
     for (auto& s : side)
         MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi));
+    for (auto& s : fin)
+        MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, lo));
+    MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&esc, cudaStreamNonBlocking, lo));
     for (auto& s : branch)
         MDZ_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     MDZ_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
@@ -398,6 +443,15 @@ int Server::init(const mdzgpu_serve_config* c)
         MDZ_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     MDZ_CUDA_TRY(cudaMalloc((void**)&d, sizeof(ServeDev)));
     MDZ_CUDA_TRY(cudaMemset(d, 0, sizeof(ServeDev)));
+    {
+        ServeStatus s0;
+        memset(&s0, 0, sizeof s0);
+        for (int c = 0; c < kServeClasses; ++c) {
+            s0.tk[0][c][0] = s0.tk[1][c][0] = ~0ull;
+            rate_adj[c] = 1.0;
+        }
+        MDZ_CUDA_TRY(cudaMemcpy(&d->status, &s0, sizeof s0, cudaMemcpyHostToDevice));
+    }
     MDZ_CUDA_TRY(cudaHostAlloc((void**)&ctl_h, sizeof(ServeCtl), cudaHostAllocDefault));
     MDZ_CUDA_TRY(cudaHostAlloc((void**)&status_h, sizeof(ServeStatus), cudaHostAllocDefault));
     MDZ_CUDA_TRY(cudaHostAlloc((void**)&req_h, sizeof(ServeReq) * kServeSlots,
@@ -416,13 +470,19 @@ int Server::init(const mdzgpu_serve_config* c)
     }
     MDZ_CUDA_TRY(cudaMalloc((void**)&arena_dev, (size_t)cfg.arena_bytes));
     MDZ_CUDA_TRY(cudaHostAlloc((void**)&stage_host, (size_t)cfg.staging_bytes,
-                               cudaHostAllocDefault));
+                               cudaHostAllocMapped));
+    MDZ_CUDA_TRY(cudaHostGetDevicePointer((void**)&stage_dev, stage_host, 0));
     arena.reset((size_t)cfg.arena_bytes);
     stage.reset((size_t)cfg.staging_bytes);
-    // one direct launch of every kernel (queues empty: they exit at once)
-    // sets their launch attributes outside the capture
-    int rc = launch_serve_perturb(d, num_sms, main);
-    for (int c = 1; !rc && c < kServeClasses; ++c)
+    // every kernel the engine may launch is loaded now, while the device
+    // is idle; one direct launch of every slice kernel (queues empty: they
+    // exit at once) sets their launch attributes outside the capture
+    int rc = preload_perturb_kernels();
+    if (!rc)
+        rc = preload_mp_kernels();
+    for (int c = 0; !rc && c < kServePerturbClasses; ++c)
+        rc = launch_serve_perturb(d, c, num_sms, main);
+    for (int c = kServePerturbClasses; !rc && c < kServeClasses; ++c)
         rc = launch_serve_mp(d, c, num_sms, main);
     if (!rc)
         rc = launch_serve_step_end(d, main);
@@ -450,16 +510,21 @@ int Server::capture_step()
     int rc = MDZGPU_OK;
     launches_per_step = 0;
     if (cudaMemcpyAsync(&d->ctl, ctl_h, sizeof(ServeCtl), cudaMemcpyHostToDevice, main)
-        != cudaSuccess
-        || cudaEventRecord(fork, main) != cudaSuccess)
+        != cudaSuccess)
+        rc = MDZGPU_ERR_CUDA;
+    if (!rc) {
+        rc = launch_serve_step_begin(d, main);
+        ++launches_per_step;
+    }
+    if (!rc && cudaEventRecord(fork, main) != cudaSuccess)
         rc = MDZGPU_ERR_CUDA;
     for (int c = 0; !rc && c < kServeClasses; ++c) {
         if (cudaStreamWaitEvent(branch[c], fork, 0) != cudaSuccess) {
             rc = MDZGPU_ERR_CUDA;
             break;
         }
-        rc = c == 0 ? launch_serve_perturb(d, num_sms, branch[c])
-                    : launch_serve_mp(d, c, num_sms, branch[c]);
+        rc = c < kServePerturbClasses ? launch_serve_perturb(d, c, num_sms, branch[c])
+                                      : launch_serve_mp(d, c, num_sms, branch[c]);
         ++launches_per_step;
         if (!rc && (cudaEventRecord(join[c], branch[c]) != cudaSuccess
                     || cudaStreamWaitEvent(main, join[c], 0) != cudaSuccess))
@@ -491,11 +556,9 @@ void Server::end(const std::shared_ptr<Req>& r, int state, int error)
         slots[r->slot] = nullptr;
         r->slot = -1;
     }
-    if (r->ev_orbit)
-        cudaEventDestroy(r->ev_orbit);
     if (r->ev_done)
         cudaEventDestroy(r->ev_done);
-    r->ev_orbit = r->ev_done = nullptr;
+    r->ev_done = nullptr;
     r->phase = kEnded;
     std::lock_guard<std::mutex> lk(mu);
     r->state = state;
@@ -552,7 +615,7 @@ void Server::check_cancels()
         }
         for (auto& s : slots)
             if (s && !s->cancel && s->timeout_ms > 0 && now - s->t_submit > s->timeout_ms
-                && s->phase != kFinishing) {
+                && s->phase == kRunning) {
                 s->cancel = true;
                 s->cancel_state = MDZGPU_REQ_TIMEOUT;
             }
@@ -650,6 +713,10 @@ int Server::setup(const std::shared_ptr<Req>& r)
         p.de = (const int*)(ob + ol.de);
         p.orbit_len = (const int*)(ob + ol.len);
         p.tiny = (const unsigned*)(ob + ol.tiny);
+        p.fractal = r->fractal;
+        p.fm = (const double*)(ob + ol.fm);
+        p.fe = (const int*)(ob + ol.fe);
+        p.axis = (const unsigned*)(ob + ol.axis);
         p.rebases = (unsigned long long*)(ob + ol.reb);
         p.lost_limit = 1.0f;  // bits a pixel may lose before its FP64 re-run
         p.flag_out = (unsigned*)(db + l.lists + 256);
@@ -676,6 +743,10 @@ int Server::setup(const std::shared_ptr<Req>& r)
         o.max_k = (int)r->depth + 1;
         o.out_len = (int*)(ob + ol.len);
         o.tiny = (unsigned*)(ob + ol.tiny);
+        o.fractal = r->fractal;
+        o.fm = (double*)(ob + ol.fm);
+        o.fe = (int*)(ob + ol.fe);
+        o.axis = (unsigned*)(ob + ol.axis);
         o.sm_busy = d->sm_busy;
         o.sm_words = kServeSmWords;
         cudaEvent_t ready;
@@ -684,18 +755,17 @@ int Server::setup(const std::shared_ptr<Req>& r)
         cudaStreamWaitEvent(side[r->slot], ready, 0);
         cudaEventDestroy(ready);
         // the orbit streams: pixels join the queue now and iterate up to
-        // the last finished entry at every step
-        int rc = launch_orbit_stream(o, prog, side[r->slot]);
+        // the last finished entry at every step; its end (1, or 2 when the
+        // finisher gave up) lands in the host word h_misc + 16
+        *hflag(r, 16) = 0;
+        int rc = launch_orbit_stream(o, prog, side[r->slot],
+                                     DoneSignal{(unsigned*)(prog + 6), dflag(r, 16)});
         if (rc)
             return rc;
-        MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_misc + 16, prog + 4, 4, cudaMemcpyDeviceToHost,
-                                     side[r->slot]));
-        MDZ_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_orbit, cudaEventDisableTiming));
-        MDZ_CUDA_TRY(cudaEventRecord(r->ev_orbit, side[r->slot]));
-        rc = launch_serve_enqueue(d, 0, (int)cur, r->slot, (unsigned)r->npix, main);
+        rc = launch_serve_enqueue(d, r->cls, (int)cur, r->slot, (unsigned)r->npix, main);
         if (rc)
             return rc;
-        qhost[0] += (long)r->npix;
+        qhost[r->cls] += (long)r->npix;
         r->orbit_running = true;
         r->phase = kRunning;
         std::lock_guard<std::mutex> lk(mu);
@@ -720,13 +790,11 @@ void Server::poll_orbits()
     for (auto& r : slots) {
         if (!r || !r->orbit_running)
             continue;
-        const cudaError_t e = cudaEventQuery(r->ev_orbit);
-        if (e == cudaErrorNotReady)
+        const int v = *hflag(r, 16);
+        if (v == 0)
             continue;
         r->orbit_running = false;
-        const int err = e != cudaSuccess
-                            ? 1
-                            : *(volatile int*)(stage_host + r->host_off + r->lay.h_misc + 16);
+        const int err = v != 1;
         if (err) {
             // the finisher gave up (or the launch failed): its pixels can not
             // finish; drop them and fail the request
@@ -740,12 +808,14 @@ void Server::poll_orbits()
 
 int Server::step()
 {
+    const double t_pre = wall_ms();
     // budgets: each running request gets an equal share of the step
     int R = 0;
     for (auto& r : slots)
         R += r && r->phase == kRunning;
     memset(ctl_h, 0, sizeof(ServeCtl));
     ctl_h->cur = cur;
+    bool steered[kServeClasses] = {};  // a budget of the class is above its floor
     {
         std::lock_guard<std::mutex> lk(mu);
         for (int s = 0; s < kServeSlots; ++s) {
@@ -757,15 +827,47 @@ int Server::step()
             unsigned left = status_h->remaining[s];
             if (left == 0 || left > r->npix)
                 left = (unsigned)r->npix;  // enqueued since the last status
-            const double b = cfg.step_ms * 1e-3 * class_rate(r->cls) / ((double)R * left);
+            const double b =
+                cfg.step_ms * 1e-3 * class_rate(r->cls) * rate_adj[r->cls] / ((double)R * left);
             const double bmin = r->cls == 0 ? 256.0 : 16.0;
             ctl_h->budget[s] = (unsigned)std::min(std::max(b, bmin), (double)(1u << 24));
+            steered[r->cls] = steered[r->cls] || b > bmin;
         }
     }
+    bool had[kServeClasses];
+    for (int c = 0; c < kServeClasses; ++c)
+        had[c] = qhost[c] > 0;
     const double t0 = wall_ms();
+    loop_ms[6] += t0 - t_pre;
     MDZ_CUDA_TRY(cudaGraphLaunch(step_exec, main));
+    loop_ms[8] += wall_ms() - t0;
     MDZ_CUDA_TRY(cudaStreamSynchronize(main));
     const double t1 = wall_ms();
+    {
+        const unsigned long long b0 = status_h->tstep[cur][0], b1 = status_h->tstep[cur][1];
+        unsigned long long first = ~0ull;
+        for (int c = 0; c < kServeClasses; ++c)
+            if (had[c])
+                first = std::min(first, status_h->tk[cur][c][0]);
+        if (b1 > b0) {
+            graph_ms += (double)(b1 - b0) * 1e-6;
+            if (first != ~0ull && first > b0)
+                lead_ms += (double)(first - b0) * 1e-6;
+        }
+    }
+    for (int c = 0; c < kServeClasses; ++c) {
+        const unsigned long long a = status_h->tk[cur][c][0], b = status_h->tk[cur][c][1];
+        if (!had[c] || a == ~0ull || b <= a)
+            continue;
+        const double ms = (double)(b - a) * 1e-6;
+        class_ms[c] += ms;
+        // fast down, slow up; the guess stays within [1e-4, 4] of itself
+        const double ratio = cfg.step_ms / std::max(ms, 1e-3);
+        const double f = ratio < 1.0 ? std::max(ratio, 0.25) : pow(std::min(ratio, 4.0), 0.25);
+        if (ratio < 1.0 && !steered[c])
+            continue;  // every budget at its floor: the time is not the budgets'
+        rate_adj[c] = std::min(std::max(rate_adj[c] * f, 1e-4), 4.0);
+    }
     cur ^= 1u;
     for (int c = 0; c < kServeClasses; ++c)
         qhost[c] = (long)status_h->qcount[c][cur];
@@ -799,60 +901,87 @@ int Server::step()
             cancel = r->cancel;
         }
         if (cancel) {
-            // the slot stream may still run the orbit: release the memory
-            // once it is idle
+            // the orbit may still run: the memory is released once it ends
             r->cancelled = true;
-            if (cudaEventCreateWithFlags(&r->ev_done, cudaEventDisableTiming) != cudaSuccess
-                || cudaEventRecord(r->ev_done, side[r->slot]) != cudaSuccess) {
-                cudaStreamSynchronize(side[r->slot]);
-                end(r, r->cancel_state, 0);
-            } else {
-                r->phase = kFinishing;
-            }
+            r->phase = kCopyWait;
             continue;
         }
+        const double tf = wall_ms();
         const int rc = start_finish(r);
+        loop_ms[7] += wall_ms() - tf;
         if (rc)
             end(r, MDZGPU_REQ_FAILED, rc);
     }
     return MDZGPU_OK;
 }
 
-// Main pass done: escalation passes (perturbation) and the copies out.
+// Main pass done.  A perturbation request whose FP32 pass flagged pixels
+// queues for the escalation passes (FP64, then multi-limb over what FP64
+// could not settle), which run one request at a time on the low-priority
+// esc stream with 1 / kEscShare of the SMs, so that a request with many
+// flagged pixels delays its own result, not the steps of the others.
+// Every other request waits only for its orbit launch to end (the arena is
+// released only once nothing writes it), then copies its results out.
 int Server::start_finish(const std::shared_ptr<Req>& r)
+{
+    // the step that finished the FP32 pass reported how many it flagged
+    const unsigned flagged = r->method == MDZGPU_METHOD_PERTURB ? status_h->flagged[r->slot] : 0u;
+    r->flagged = flagged;
+    if (flagged != 0) {
+        esc_fifo.push_back(r);
+        r->phase = kEscWait;
+    } else {
+        memset(stage_host + r->host_off + r->lay.h_misc, 0, 8);  // no escalation
+        r->phase = kCopyWait;
+    }
+    return MDZGPU_OK;
+}
+
+// One chunk of an escalation pass: list tiles esc_base + [0, chunk), on
+// 1 / kEscShare of the SMs while other requests run, on all of them when
+// the passes are the only work left.
+int Server::launch_escalation(const std::shared_ptr<Req>& r, bool mp_pass)
 {
     const Layout& l = r->lay;
     char* db = arena_dev + r->dev_off;
-    char* hb = stage_host + r->host_off;
-    cudaStream_t s = side[r->slot];
-    int launches = 0;
-    if (r->method == MDZGPU_METHOD_PERTURB) {
-        mdzgpu_ctx shape;  // the list passes read only the SM count
-        shape.device = device;
-        shape.num_sms = num_sms;
-        PerturbLaunch p = req_h[r->slot].pl;
-        unsigned* counts_dev = (unsigned*)(db + l.lists);
-        unsigned* list1 = (unsigned*)(db + l.lists + 256);
-        unsigned* list2 = list1 + r->npix;
-        MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, s));
+    bool alone;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        alone = waiting.empty();
+    }
+    for (const auto& o : slots)
+        alone = alone && (!o || o->phase > kRunning);
+    mdzgpu_ctx shape;  // the list passes read only the SM count
+    shape.device = device;
+    shape.num_sms = alone ? num_sms : std::max(1, num_sms / kEscShare);
+    const unsigned chunk = (unsigned)shape.num_sms * kEscTilesPerSm;
+    PerturbLaunch p = req_h[r->slot].pl;
+    unsigned* counts_dev = (unsigned*)(db + l.lists);
+    unsigned* list1 = (unsigned*)(db + l.lists + 256);
+    unsigned* list2 = list1 + r->npix;
+    // the sync block (tile counter, exit count at +128) starts at zero
+    MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, esc));
+    const DoneSignal done{(unsigned*)(db + l.sync + 128), dflag(r, mp_pass ? 24 : 20)};
+    *hflag(r, mp_pass ? 24 : 20) = 0;
+    int rc;
+    if (!mp_pass) {
         p.list_in = list1;
         p.list_in_count = counts_dev;
         p.lost_limit = 6.0f;  // FP64 pass: bits before the multi-limb re-run
         p.flag_out = list2;
         p.flag_out_count = counts_dev + 1;
-        int rc = launch_perturb(&shape, p, s, 1);
-        if (rc) {
-            shape.stream = nullptr;
-            return rc;
-        }
-        MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, s));
+        p.done = done;
+        p.tile_base = r->esc_base;
+        p.tile_limit = chunk;
+        rc = launch_perturb(&shape, p, esc, 1);
+    } else {
         MpLaunch q;
         q.W = r->W;
         q.H = r->H;
         q.row0 = 0;
         q.nrows = r->H;
         q.family = MDZ_FAMILY_MANDEL;
-        q.fractal = MDZ_MANDELBROT;
+        q.fractal = r->fractal;
         q.depth = r->depth;
         q.words = r->words;
         q.xs = (const uint32_t*)(db + l.tables);
@@ -866,12 +995,30 @@ int Server::start_finish(const std::shared_ptr<Req>& r)
         q.list = list2;
         q.list_count = counts_dev + 1;
         q.mag = p.mag;
-        rc = launch_mp(&shape, q, s);
-        shape.stream = nullptr;
-        if (rc)
-            return rc;
-        launches += 2;
-        MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_misc, counts_dev, 8, cudaMemcpyDeviceToHost, s));
+        q.done = done;
+        q.tile_base = r->esc_base;
+        q.tile_limit = chunk;
+        rc = launch_mp(&shape, q, esc);
+    }
+    r->esc_base += chunk;
+    if (!rc) {
+        std::lock_guard<std::mutex> lk(mu);
+        st.launches += 1;
+    }
+    return rc;
+}
+
+// Copies out on the request's fin stream (nothing long runs before them).
+int Server::enqueue_copies(const std::shared_ptr<Req>& r)
+{
+    const Layout& l = r->lay;
+    char* db = arena_dev + r->dev_off;
+    char* hb = stage_host + r->host_off;
+    cudaStream_t s = fin[r->slot];
+    if (r->method == MDZGPU_METHOD_PERTURB) {
+        if (r->phase == kEscMp)  // escalated: the lists' counts
+            MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_misc, db + l.lists, 8, cudaMemcpyDeviceToHost,
+                                         s));
         MDZ_CUDA_TRY(cudaMemcpyAsync(hb + l.h_misc + 8, db + l.orbit + l.ol.reb, 8,
                                      cudaMemcpyDeviceToHost, s));
     }
@@ -883,8 +1030,67 @@ int Server::start_finish(const std::shared_ptr<Req>& r)
     MDZ_CUDA_TRY(cudaEventCreateWithFlags(&r->ev_done, cudaEventDisableTiming));
     MDZ_CUDA_TRY(cudaEventRecord(r->ev_done, s));
     r->phase = kFinishing;
-    std::lock_guard<std::mutex> lk(mu);
-    st.launches += launches;
+    return MDZGPU_OK;
+}
+
+int Server::advance_finishing()
+{
+    // results of requests whose kernels have all ended
+    for (auto& slot_ref : slots) {
+        auto r = slot_ref;
+        if (!r || r->phase != kCopyWait || r->orbit_running)
+            continue;
+        if (r->cancelled) {
+            end(r, r->cancel_state, 0);
+            continue;
+        }
+        if (int rc = enqueue_copies(r))
+            end(r, MDZGPU_REQ_FAILED, rc);
+    }
+    // the escalation chunk in flight: 1 = more of the list is left, 3 = the
+    // pass reached the list's end
+    if (esc_cur) {
+        auto r = esc_cur;
+        const int v = *hflag(r, r->phase == kEscFp64 ? 20 : 24);
+        int rc = MDZGPU_OK;
+        if (v == 1) {
+            rc = launch_escalation(r, r->phase == kEscMp);
+        } else if (v == 3 && r->phase == kEscFp64) {
+            r->phase = kEscMp;
+            r->esc_base = 0;
+            rc = launch_escalation(r, true);
+        } else if (v == 3) {
+            esc_cur = nullptr;
+            rc = enqueue_copies(r);
+        }
+        if (rc) {
+            esc_cur = nullptr;
+            end(r, MDZGPU_REQ_FAILED, rc);
+        }
+    }
+    // the next one: the least work (flagged pixels x depth) among those
+    // whose orbit ended
+    if (!esc_cur) {
+        auto best = esc_fifo.end();
+        for (auto it = esc_fifo.begin(); it != esc_fifo.end(); ++it) {
+            if ((*it)->orbit_running)
+                continue;
+            if (best == esc_fifo.end()
+                || (double)(*it)->flagged * (*it)->depth < (double)(*best)->flagged * (*best)->depth)
+                best = it;
+        }
+        if (best != esc_fifo.end()) {
+            auto r = *best;
+            esc_fifo.erase(best);
+            esc_cur = r;
+            r->phase = kEscFp64;
+            r->esc_base = 0;
+            if (int rc = launch_escalation(r, false)) {
+                esc_cur = nullptr;
+                end(r, MDZGPU_REQ_FAILED, rc);
+            }
+        }
+    }
     return MDZGPU_OK;
 }
 
@@ -944,38 +1150,62 @@ void Server::run()
             if (quit)
                 break;
         }
+        double ta = wall_ms();
         check_cancels();
+        double tb = wall_ms();
+        loop_ms[0] += tb - ta;
         admit();
+        ta = wall_ms();
+        loop_ms[1] += ta - tb;
         poll_orbits();
+        tb = wall_ms();
+        loop_ms[2] += tb - ta;
         long queued = 0;
         for (long q : qhost)
             queued += q;
         if (queued > 0) {
-            if (step()) {
+            const int step_rc = step();
+            ta = wall_ms();
+            loop_ms[3] += ta - tb;
+            tb = ta;
+            if (step_rc) {
                 // a failed step leaves the device state unknown: fail everything
+                cudaStreamSynchronize(esc);
+                esc_fifo.clear();
+                esc_cur = nullptr;
                 for (auto& s : slots)
                     if (s) {
                         auto keep = s;
                         cudaStreamSynchronize(side[keep->slot]);
+                        cudaStreamSynchronize(fin[keep->slot]);
                         end(keep, MDZGPU_REQ_FAILED, MDZGPU_ERR_CUDA);
                     }
                 for (long& q : qhost)
                     q = 0;
             }
         }
+        advance_finishing();
         poll_finishing();
+        ta = wall_ms();
+        loop_ms[4] += ta - tb;
         if (queued == 0) {
             bool waiting_gpu = false;
             for (const auto& s : slots)
-                waiting_gpu = waiting_gpu || (s && (s->orbit_running || s->phase == kFinishing));
+                waiting_gpu = waiting_gpu || (s && (s->orbit_running || s->phase > kRunning));
             if (waiting_gpu)
                 std::this_thread::sleep_for(std::chrono::microseconds(100));
+            loop_ms[5] += wall_ms() - ta;
         }
     }
     // shutdown: let the GPU work in flight end, then cancel what is left
     cudaStreamSynchronize(main);
     for (auto& s : side)
         cudaStreamSynchronize(s);
+    for (auto& s : fin)
+        cudaStreamSynchronize(s);
+    cudaStreamSynchronize(esc);
+    esc_fifo.clear();
+    esc_cur = nullptr;
     for (auto& s : slots)
         if (s) {
             auto keep = s;
@@ -1017,6 +1247,11 @@ void Server::teardown()
     for (auto& s : side)
         if (s)
             cudaStreamDestroy(s);
+    for (auto& s : fin)
+        if (s)
+            cudaStreamDestroy(s);
+    if (esc)
+        cudaStreamDestroy(esc);
     if (main)
         cudaStreamDestroy(main);
     cudaFree(arena_dev);
@@ -1026,8 +1261,23 @@ void Server::teardown()
     cudaFreeHost(ctl_h);
     cudaFreeHost(status_h);
     cudaFreeHost(req_h);
-    if (log)
+    if (log) {
+        fprintf(log,
+                "{\"loop_ms\": {\"cancels\": %.1f, \"admit\": %.1f, \"orbits\": %.1f, "
+                "\"step\": %.1f, \"finish\": %.1f, \"idle\": %.1f, \"step_pre_graph\": %.1f, "
+                "\"step_start_finish\": %.1f, \"graph_launch\": %.1f}, ",
+                loop_ms[0], loop_ms[1], loop_ms[2], loop_ms[3], loop_ms[4], loop_ms[5],
+                loop_ms[6], loop_ms[7], loop_ms[8]);
+        fprintf(log, "\"device_step_ms\": %.3f, \"step_lead_ms\": %.3f, \"slice_kernel_ms\": [",
+                graph_ms, lead_ms);
+        for (int c = 0; c < kServeClasses; ++c)
+            fprintf(log, "%s%.3f", c ? ", " : "", class_ms[c]);
+        fprintf(log, "], \"rate_adjust\": [");
+        for (int c = 0; c < kServeClasses; ++c)
+            fprintf(log, "%s%.4g", c ? ", " : "", rate_adj[c]);
+        fprintf(log, "]}\n");
         fclose(log);
+    }
 }
 
 }  // namespace mdz

@@ -8,6 +8,7 @@ the reference sources exist; the GPU machine only reads the outputs).
   python tests/golden/make_golden.py abi       # abi_layout.json (reference struct offsets)
   python tests/golden/make_golden.py centres   # serve_centres.json (serving stream centres)
   python tests/golden/make_golden.py colour    # colour.npz (reference palette_apply / AA)
+  python tests/golden/make_golden.py perturb_fold  # perturb_fold.npz (ship / celtic, MPFR 2p)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -483,6 +484,61 @@ def make_perturb() -> None:
     (GOLD / "perturb_views.json").write_text(json.dumps(meta, indent=1))
 
 
+def make_perturb_fold() -> None:
+    """Burning ship and celtic frames for the folded perturbation, scored
+    against MPFR at twice the precision.  The deep views sit at the serving
+    pool's boundary points of each formula.  Near those points the folded
+    maps are often chaotic: MPFR at p, 2p and 3p bits then give different
+    counts for many pixels, so no computation at the view's precision can
+    match pixel by pixel.  Each frame therefore stores the counts at p, 2p
+    and 3p bits and a kind: "resolved" (the three agree on >= 99% of
+    pixels: pixel-level parity applies) or "chaotic" (the score is the
+    agreement rate with 2p, against the reference's own at p)."""
+    pool = json.loads((GOLD / "serve_centres.json").read_text())["centres"]
+    ship = [c for c in pool if c["fractal"] == 1]
+    celtic = [c for c in pool if c["fractal"] == 2]
+    P = Fraction(2)
+    frames = [
+        ("f_ship_shallow", 1, "-1.7626", "-0.0281", 48, 36, 2000, Fraction(1, 100), 64),
+        ("f_celtic_shallow", 2, "-0.8", "0.15", 48, 36, 2000, Fraction(1, 5), 64),
+        ("f_ship_a300", 1, ship[3]["cx"], ship[3]["cy"], 48, 36, 10000, P ** -300, 364),
+        ("f_ship_b700", 1, ship[4]["cx"], ship[4]["cy"], 32, 24, 10000, P ** -700, 764),
+        ("f_ship_c300", 1, ship[1]["cx"], ship[1]["cy"], 48, 36, 3000, P ** -300, 364),
+        ("f_celtic_a300", 2, celtic[0]["cx"], celtic[0]["cy"], 48, 36, 3000, P ** -300, 364),
+        ("f_celtic_b300", 2, celtic[2]["cx"], celtic[2]["cy"], 48, 36, 3000, P ** -300, 364),
+        ("f_ship_chaos100", 1, ship[0]["cx"], ship[0]["cy"], 48, 36, 4000, P ** -100, 164),
+        ("f_celtic_chaos1000", 2, celtic[2]["cx"], celtic[2]["cy"], 32, 24, 12000, P ** -1000,
+         1064),
+    ]
+    out, meta = {}, {}
+    for name, fr, scx, scy, W, H, depth, width, prec in frames:
+        cx = MpVal.from_fraction(parse_num(scx), prec).to_fraction()
+        cy = MpVal.from_fraction(parse_num(scy), prec).to_fraction()
+        width = MpVal.from_fraction(width, prec).to_fraction()
+        t0 = time.time()
+        cre, cim = [], []
+        for ln in range(H):
+            for ix in range(W):
+                x, y = perturb_c(cx, cy, width, W, H, ix, ln)
+                cre.append(hexfloat(x))
+                cim.append(hexfloat(y))
+        c1, _ = O.points_mpfr(cre, cim, depth, prec, fractal=fr, threads=THREADS)
+        c2, m2 = O.points_mpfr(cre, cim, depth, 2 * prec, fractal=fr, threads=THREADS)
+        c3, _ = O.points_mpfr(cre, cim, depth, 3 * prec, fractal=fr, threads=THREADS)
+        agree = float(((c1 == c2) & (c2 == c3)).mean())
+        out[name] = c2.reshape(H, W).astype(np.int32)
+        out[name + "__p"] = c1.reshape(H, W).astype(np.int32)
+        out[name + "__3p"] = c3.reshape(H, W).astype(np.int32)
+        out[name + "__mag"] = m2.reshape(H, W)
+        meta[name] = dict(fractal=fr, cx=hexfloat(cx), cy=hexfloat(cy), width=hexfloat(width),
+                          W=W, H=H, depth=depth, prec=prec, oracle_prec=2 * prec,
+                          kind="resolved" if agree >= 0.99 else "chaotic")
+        print(f"{name}: {time.time() - t0:.1f}s distinct counts {len(np.unique(c2))} "
+              f"p = 2p = 3p on {agree:.4f} -> {meta[name]['kind']}", flush=True)
+    np.savez_compressed(GOLD / "perturb_fold.npz", **out)
+    (GOLD / "perturb_fold_views.json").write_text(json.dumps(meta, indent=1))
+
+
 def parse_num(s):
     from mdz_gb300.mpval import parse_number
     return parse_number(s)
@@ -507,7 +563,8 @@ def main(argv: list[str]) -> None:
     what = argv[1:] or ["fp64"]
     for w in what:
         {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
-         "perturb": make_perturb, "centres": make_centres, "colour": make_colour}[w]()
+         "perturb": make_perturb, "centres": make_centres, "colour": make_colour,
+         "perturb_fold": make_perturb_fold}[w]()
 
 
 if __name__ == "__main__":

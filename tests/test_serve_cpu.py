@@ -31,11 +31,13 @@ def test_footprint_perturbation_layout():
     L = native.load().mdzgpu_perturb_limbs(300)
     entries = 5002
     orbit = (al(entries * 16) + al(entries * 16) + al(entries * 4) + al(entries * 8)
+             + al(entries * 4) + al((entries // 32 + 40) * 4) + al(entries * 8)
              + al(entries * 4) + al((entries // 32 + 40) * 4) + 256 + al(2 * L * 4) + 256
              + al(entries * 2 * L * 4))
     # counts, |z|^2, 32-byte pixel state, two escalation lists, sync, orbit
-    # (zf, zd, ze, dd, de, tiny-|Z| bit mask, progress, centre, rebases, raw
-    # digits), escalation-pass coordinates
+    # (zq, zd, ze, dd, de, tiny-|Z| bit mask, fold value fm / fe, fold-axis
+    # bit mask, progress, centre, rebases, raw digits), escalation-pass
+    # coordinates
     words = 12   # 300 + 40 bits -> 11 words -> even
     expect = (al(4 * n) + al(4 * n) + al(32 * n) + al(256 + 8 * n) + 256 + al(orbit)
               + al((100 + 60) * words * 4))
@@ -44,15 +46,15 @@ def test_footprint_perturbation_layout():
 
 
 def test_footprint_multi_limb_scales_with_words():
-    d1, _ = footprint(req(fractal=1, prec=128))
-    d2, _ = footprint(req(fractal=1, prec=1000))
+    d1, _ = footprint(req(fractal=3, prec=128))
+    d2, _ = footprint(req(fractal=3, prec=1000))
     assert d2 > 3 * d1
-    d3, _ = footprint(req(fractal=0, method="multi_limb", prec=128))
+    d3, _ = footprint(req(fractal=1, method="multi_limb", prec=128))
     assert d3 == d1
 
 
 @pytest.mark.parametrize("kw", [
-    dict(fractal=1, method="perturbation"),   # perturbation is Mandelbrot-only
+    dict(fractal=3, method="perturbation"),   # no perturbation for the hybrid
     dict(prec=4000, fractal=1),               # beyond the multi-limb words
     dict(W=0),
     dict(depth=0),

@@ -219,7 +219,7 @@ def test_serve_timeout(server):
 
 def test_serve_rejects_bad_requests(server):
     bad = view_request("p_gal_polyp", method="perturbation")
-    bad.fractal = 1                     # perturbation is Mandelbrot-only
+    bad.fractal = 3                     # no perturbation for the hybrid
     with pytest.raises(ServeError):
         server.submit(bad)
     deep = region_request(1, "-1.7626", "-0.0281", "0.01", 16, 16, 100, 4000)
