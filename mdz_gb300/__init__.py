@@ -134,8 +134,9 @@ class Renderer:
     # -- perturbation ---------------------------------------------------------
     def render_perturb(self, W: int, H: int, depth: int, cx: MpVal, cy: MpVal, width: MpVal,
                        precision: int, limbs: int = 0, want_mag: bool = False,
-                       out: np.ndarray | None = None, mag: np.ndarray | None = None):
-        f = Frame(W, H, 0, 0, depth)
+                       out: np.ndarray | None = None, mag: np.ndarray | None = None,
+                       fractal: int = 0):
+        f = Frame(W, H, 0, fractal, depth)
         if out is None:
             out = np.empty((H, W), np.int32)
         if want_mag and mag is None:

@@ -1048,6 +1048,36 @@ __device__ __forceinline__ void fold_fast_step(PixState<T>& st, T Zx, T Zy, T fs
     }
 }
 
+// The rest of a folded-formula pixel whose FP64 error estimate is lost
+// (its orbit is chaotic beyond the pass's precision): the deltas no longer
+// carry the pixel's offset from the reference (the error is far above dc),
+// so its own orbit z' = f(z) + c is iterated directly in FP64, which gives
+// the same kind of trajectory without the rebases and orbit reads that
+// perturbation needs once z is far from the reference.  z = z_wz; runs
+// iterations wz + 1 .. depth.  Returns the count (0: did not escape).
+template <int FR>
+__device__ uint32_t fold_direct(double xr, double xi, double cr, double ci, uint32_t wz,
+                                uint32_t depth, float& mag)
+{
+    for (uint32_t w = wz + 1; w <= depth; ++w) {
+        const double a = xr * xr - xi * xi, b = xr * xi;
+        if (FR == MDZ_BURNING_SHIP) {
+            xr = a + cr;
+            xi = 2.0 * fabs(b) + ci;
+        } else {
+            xr = fabs(a) + cr;
+            xi = 2.0 * b + ci;
+        }
+        const double m2 = xr * xr + xi * xi;
+        if (m2 > 4.0) {
+            mag = (float)m2;
+            return w;
+        }
+    }
+    mag = (float)(xr * xr + xi * xi);
+    return 0;
+}
+
 // How a pixel learns which reference-orbit entries it may read:
 //   kOrbitComplete  the orbit is finished: K = *orbit_len entries;
 //   kOrbitWait      fused launch: wait (bounded) for the finisher;
@@ -1278,11 +1308,14 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
             if (FR != MDZ_MANDELBROT) {
                 // with dz below the T range (s = 0) a fold is out of reach
                 // unless the entry is marked: the same choice as the blocks
+                // (a lost estimate leaves only the rounding margin: the side
+                // is still decided exactly, its error no longer matters)
                 const bool fast =
                     !careful && !axis_bit(p, m)
                     && (st.s == (T)0
-                        || fold_certain<T, FR>(zr, zi, Zx, Zy, fs,
-                                               st.sm * fmax(fabs(st.tr), fabs(st.ti))));
+                        || fold_certain<T, FR>(
+                            zr, zi, Zx, Zy, fs,
+                            lost_track ? (T)0 : st.sm * fmax(fabs(st.tr), fabs(st.ti))));
                 if (fast) {
                     fold_fast_step<T, FR>(st, Zx, Zy, fs);
                 } else {
@@ -1313,9 +1346,10 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 st.e2 = Mant<T>::fma_(g, st.e2, Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti));
         }
         if (kTrack) {
-            // the band widens to 2^9 err where the error estimate of z is larger
+            // the band widens to 2^9 err where the error estimate of z is
+            // larger (not once the estimate is lost: its decisions stand)
             const T dv = magT - (T)4;
-            if (dv > -(T)6.1035156e-5 || dv * dv <= st.kb * st.e2) {
+            if (dv > -(T)6.1035156e-5 || (!lost_track && dv * dv <= st.kb * st.e2)) {
                 bool unsure;
                 const bool esc = escape_fold<T>(p, m, st, unsure);
                 if (unsure && !lost_track)
@@ -1375,6 +1409,18 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 r.mag = (float)magT;
                 count = 0;
                 return 1;  // the next pass redoes the pixel
+            }
+            if (FR != MDZ_MANDELBROT && sizeof(T) == 8 && MODE == kOrbitComplete && lost_track
+                && last == p.depth) {
+                // c = Z_1 + dc
+                const double cr = ldexp(p.zd[1].x, p.ze[1]) + ldexp(dcm_r, dce);
+                const double ci = ldexp(p.zd[1].y, p.ze[1]) + ldexp(dcm_i, dce);
+                float mg = 0.f;
+                count = fold_direct<FR>((double)zr, (double)zi, cr, ci, wz, p.depth, mg);
+                r.mag = mg;
+                r.m = m;
+                r.wz = p.depth + 1;
+                return 1;
             }
         }
         ++wz;
