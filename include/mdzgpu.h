@@ -306,7 +306,8 @@ int mdzgpu_abi_layout(int64_t* out, int n);
 typedef struct mdzgpu_server mdzgpu_server;
 
 enum {
-    MDZGPU_METHOD_AUTO = 0,       /* perturbation for the Mandelbrot formula,
+    MDZGPU_METHOD_AUTO = 0,       /* perturbation for the Mandelbrot, burning
+                                     ship and generalized celtic formulas,
                                      multi-limb otherwise */
     MDZGPU_METHOD_PERTURB = 1,    /* as mdzgpu_render_perturb */
     MDZGPU_METHOD_MULTI_LIMB = 2  /* multi-limb fixed point, perturbation
