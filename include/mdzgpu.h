@@ -339,7 +339,7 @@ typedef struct mdzgpu_serve_config {
  * that must stay valid until the request leaves the RUNNING state. */
 typedef struct mdzgpu_request {
     int32_t width, height;
-    int32_t family, fractal;      /* MDZ_FAMILY_MANDEL; any MDZ formula */
+    int32_t family, fractal;      /* MDZ_FAMILY_MANDEL / _JULIA; any MDZ formula */
     int64_t depth;
     int64_t precision;
     mdzgpu_mpval cx, cy, span;
@@ -348,6 +348,9 @@ typedef struct mdzgpu_request {
     double timeout_ms;            /* from submission; 0 = none */
     int32_t* counts;
     float* mag2;
+    /* Julia family: the constant c (z0 is the pixel); the multi-limb kernel
+     * serves it (MDZGPU_METHOD_AUTO picks it) */
+    mdzgpu_mpval julia_re, julia_im;
 } mdzgpu_request;
 
 typedef struct mdzgpu_request_status {

@@ -300,6 +300,9 @@ __global__ void __launch_bounds__(block_threads<N>()) serve_mp_kernel(ServeDev* 
                 const int ix = (int)(pix - (unsigned)line * (unsigned)W);
                 const uint32_t* xs = rq.xs + (size_t)ix * N;
                 const uint32_t* ys = rq.ys + (size_t)line * N;
+                // c: the pixel (Mandelbrot family) or the Julia constant
+                const uint32_t* cxs = rq.julia ? rq.julia : xs;
+                const uint32_t* cys = rq.julia ? rq.julia + N : ys;
                 uint32_t* sp = (uint32_t*)(rq.state + (size_t)pix * rq.state_stride);
                 uint32_t wre[N], wim[N], sre, sim, wz;
                 if (e & kEntryFresh) {
@@ -332,8 +335,8 @@ __global__ void __launch_bounds__(block_threads<N>()) serve_mp_kernel(ServeDev* 
                     uint32_t* cim = smem + (size_t)N * stride + threadIdx.x;
 #pragma unroll
                     for (int k = 0; k < N; ++k) {
-                        cre[k * stride] = xs[k];
-                        cim[k * stride] = ys[k];
+                        cre[k * stride] = cxs[k];
+                        cim[k * stride] = cys[k];
                     }
                     CShared<N> gr{cre, stride}, gi{cim, stride};
                     fin = escape_mp_resume<N>(wre, wim, sre, sim, gr, gi, rq.fractal, wz, last,
@@ -342,8 +345,8 @@ __global__ void __launch_bounds__(block_threads<N>()) serve_mp_kernel(ServeDev* 
                     CRegs<N> gr, gi;
 #pragma unroll
                     for (int k = 0; k < N; ++k) {
-                        gr.w[k] = xs[k];
-                        gi.w[k] = ys[k];
+                        gr.w[k] = cxs[k];
+                        gi.w[k] = cys[k];
                     }
                     fin = escape_mp_resume<N>(wre, wim, sre, sim, gr, gi, rq.fractal, wz, last,
                                               depth, mag);

@@ -57,6 +57,7 @@ struct ServeReq {
     const uint32_t* xs;       // multi-limb: [W][words] pixel x
     const uint32_t* ys;       // multi-limb: [H][words] pixel y
     int fractal;              // multi-limb formula (MDZ_MANDELBROT ...)
+    const uint32_t* julia;    // multi-limb, Julia family: [2][words] c; else null
     int words;
     uint4* state;             // resumable per-pixel state, indexed by pixel
     unsigned state_stride;    // uint4 per pixel

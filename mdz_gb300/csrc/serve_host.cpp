@@ -128,6 +128,7 @@ struct Req {
     int limbs = 0;         // orbit digits (perturbation)
     size_t npix = 0;
     bool want_mag = false;
+    bool julia = false;           // Julia family (multi-limb): c follows the tables
     int32_t* out_counts = nullptr;
     float* out_mag = nullptr;
     double timeout_ms = 0;
@@ -179,11 +180,11 @@ Layout make_layout(const Req& r)
         o += al(l.ol.bytes);
     }
     l.tables = o;
-    o += al((size_t)(r.W + r.H) * r.words * 4);
+    o += al(r.tables.size() * 4);
     l.dev_bytes = o;
     size_t h = 0;
     l.h_tables = h;
-    h += al((size_t)(r.W + r.H) * r.words * 4);
+    h += al(r.tables.size() * 4);
     l.h_digits = h;
     h += al(2 * (size_t)r.limbs * 4 + 4);
     l.h_counts = h;
@@ -214,9 +215,9 @@ int prepare(const mdzgpu_request* q, Req& r)
         set_error("serve: depth %lld outside [1, 2^31 - 2]", (long long)q->depth);
         return MDZGPU_ERR_ARG;
     }
-    if (q->family != MDZ_FAMILY_MANDEL) {
-        set_error("serve: only the Mandelbrot family is served");
-        return MDZGPU_ERR_UNSUPPORTED;
+    if (q->family != MDZ_FAMILY_MANDEL && q->family != MDZ_FAMILY_JULIA) {
+        set_error("serve: unknown family %d", q->family);
+        return MDZGPU_ERR_ARG;
     }
     if (q->fractal < MDZ_MANDELBROT || q->fractal > MDZ_VARIANT) {
         set_error("serve: unknown formula %d", q->fractal);
@@ -229,14 +230,21 @@ int prepare(const mdzgpu_request* q, Req& r)
     int method = q->method;
     // perturbation for the Mandelbrot, burning ship and celtic formulas; the
     // hybrid (its formula alternates per iteration) on the multi-limb kernel
+    // (and the Julia family, z0 = pixel, on the multi-limb kernel)
     if (method == MDZGPU_METHOD_AUTO)
-        method = q->fractal == MDZ_VARIANT ? MDZGPU_METHOD_MULTI_LIMB : MDZGPU_METHOD_PERTURB;
+        method = q->fractal == MDZ_VARIANT || q->family == MDZ_FAMILY_JULIA
+                     ? MDZGPU_METHOD_MULTI_LIMB
+                     : MDZGPU_METHOD_PERTURB;
     if (method != MDZGPU_METHOD_PERTURB && method != MDZGPU_METHOD_MULTI_LIMB) {
         set_error("serve: unknown method %d", q->method);
         return MDZGPU_ERR_ARG;
     }
     if (method == MDZGPU_METHOD_PERTURB && q->fractal == MDZ_VARIANT) {
         set_error("serve: perturbation is not implemented for the mandel-celtic hybrid");
+        return MDZGPU_ERR_UNSUPPORTED;
+    }
+    if (method == MDZGPU_METHOD_PERTURB && q->family == MDZ_FAMILY_JULIA) {
+        set_error("serve: perturbation serves the Mandelbrot family only");
         return MDZGPU_ERR_UNSUPPORTED;
     }
     if (!q->counts) {
@@ -288,10 +296,20 @@ int prepare(const mdzgpu_request* q, Req& r)
     int rc = half_spacing(&q->span, r.W, &r.hs_m, &r.hs_e);
     if (rc)
         return rc;
-    r.tables.assign((size_t)(r.W + r.H) * r.words, 0);
+    r.julia = q->family == MDZ_FAMILY_JULIA;
+    r.tables.assign((size_t)(r.W + r.H + (r.julia ? 2 : 0)) * r.words, 0);
     if (perturb_tables(&q->cx, &q->cy, r.hs_m, r.hs_e, r.W, r.H, r.words, r.tables)) {
         set_error("serve: pixel coordinates must satisfy |x|, |y| < 4");
         return MDZGPU_ERR_RANGE;
+    }
+    if (r.julia) {
+        uint32_t* jw = r.tables.data() + (size_t)(r.W + r.H) * r.words;
+        if (fx_from_mpval(&q->julia_re, r.words, jw)
+            || fx_from_mpval(&q->julia_im, r.words, jw + r.words)
+            || !fx_fits_coordinate(jw, r.words) || !fx_fits_coordinate(jw + r.words, r.words)) {
+            set_error("serve: the Julia constant must satisfy |re|, |im| < 4");
+            return MDZGPU_ERR_RANGE;
+        }
     }
     r.lay = make_layout(r);
     return MDZGPU_OK;
@@ -694,6 +712,7 @@ int Server::setup(const std::shared_ptr<Req>& r)
     p.sync = (FrameSync*)(db + l.sync);
     q.xs = (const uint32_t*)(db + l.tables);
     q.ys = q.xs + (size_t)r->W * r->words;
+    q.julia = r->julia ? q.xs + (size_t)(r->W + r->H) * r->words : nullptr;
     q.fractal = r->fractal;
     q.words = r->words;
     q.state = (uint4*)(db + l.state);

@@ -57,7 +57,8 @@ class Request(C.Structure):
                 ("fractal", C.c_int32), ("depth", C.c_int64), ("precision", C.c_int64),
                 ("cx", MpValStruct), ("cy", MpValStruct), ("span", MpValStruct),
                 ("method", C.c_int32), ("pad", C.c_int32), ("timeout_ms", C.c_double),
-                ("counts", C.c_void_p), ("mag2", C.c_void_p)]
+                ("counts", C.c_void_p), ("mag2", C.c_void_p),
+                ("julia_re", MpValStruct), ("julia_im", MpValStruct)]
 
 
 class RequestStatus(C.Structure):

@@ -40,6 +40,8 @@ class RenderRequest:
     fractal: int = 0
     method: str = "auto"
     want_mag: bool = False
+    family: int = 0                              # 1: Julia (z0 = pixel, c = julia)
+    julia: tuple[MpVal, MpVal] | None = None
     timeout_ms: float = 0.0
     counts: np.ndarray | None = None
     mag: np.ndarray | None = None
@@ -50,11 +52,14 @@ class RenderRequest:
             self.counts = np.zeros((self.height, self.width), np.int32)
         if self.want_mag and self.mag is None:
             self.mag = np.zeros((self.height, self.width), np.float32)
-        mp = [v.struct() for v in (self.cx, self.cy, self.span)]
+        vals = [self.cx, self.cy, self.span] + (list(self.julia) if self.julia else [])
+        mp = [v.struct() for v in vals]
         self._keep = [k for _, k in mp]
         r = native.Request()
         r.width, r.height = self.width, self.height
-        r.family, r.fractal = 0, self.fractal
+        r.family, r.fractal = self.family, self.fractal
+        if self.julia:
+            r.julia_re, r.julia_im = mp[3][0], mp[4][0]
         r.depth, r.precision = self.depth, self.precision
         r.cx, r.cy, r.span = mp[0][0], mp[1][0], mp[2][0]
         r.method = METHOD[self.method]

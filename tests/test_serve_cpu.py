@@ -53,6 +53,32 @@ def test_footprint_multi_limb_scales_with_words():
     assert d3 == d1
 
 
+def julia_req(method="auto", jre="-0.8", prec=128, W=64, H=48):
+    r = req(W=W, H=H, prec=prec, method=method, span="1.5")
+    r.family = 1
+    r.julia = (MpVal.from_fraction(Fraction(jre), prec), MpVal.from_fraction(Fraction("0.156"),
+                                                                              prec))
+    return r
+
+
+def test_footprint_julia_adds_the_constant():
+    # the Julia family runs on the multi-limb kernel: its coordinate tables
+    # carry the constant's two numbers after the pixel rows
+    dj, _ = footprint(julia_req())
+    dm, _ = footprint(req(W=64, H=48, prec=128, method="multi_limb", span="1.5"))
+    words = 6   # 128 + 40 bits -> 6 words
+    assert dj - dm == al((64 + 48 + 2) * words * 4) - al((64 + 48) * words * 4)
+
+
+@pytest.mark.parametrize("kw", [
+    dict(method="perturbation"),   # perturbation serves the Mandelbrot family
+    dict(jre="4.5"),               # constant out of range
+])
+def test_footprint_rejects_julia(kw):
+    with pytest.raises(ServeError):
+        footprint(julia_req(**kw))
+
+
 @pytest.mark.parametrize("kw", [
     dict(fractal=3, method="perturbation"),   # no perturbation for the hybrid
     dict(prec=4000, fractal=1),               # beyond the multi-limb words

@@ -158,6 +158,39 @@ def test_serve_multi_limb_vs_mpfr_2x(server, fractal, cx, cy, span, prec):
     assert len(np.unique(want)) > 10
 
 
+@pytest.mark.parametrize("fractal,jre,jim,cx,cy,span,prec", [
+    (0, "-0.8", "0.156", "0", "0", "1.5", 128),
+    (1, "-1.75", "-0.03", "0", "0", "2", 96),
+    (2, "-0.9", "0.2", "0.1", "0.1", "1.5", 160),
+])
+def test_serve_julia_vs_mpfr_2x(server, fractal, jre, jim, cx, cy, span, prec):
+    """Julia family (z0 = pixel, c = the constant) through the multi-limb
+    slice kernel, picked by the automatic method."""
+    from oracle import oracle as O
+    W, H, depth = 32, 24, 1500
+    jr = MpVal.from_fraction(Fraction(jre), prec)
+    ji = MpVal.from_fraction(Fraction(jim), prec)
+    req = region_request(fractal, cx, cy, span, W, H, depth, prec)
+    req.method = "auto"
+    req.family = 1
+    req.julia = (jr, ji)
+    st = run_alone(server, req)
+    assert st["method"] == 2   # multi-limb
+    zre, zim = [], []
+    for line in range(H):
+        for ix in range(W):
+            a, b = perturb_pixel_c(req.cx, req.cy, req.span, W, H, ix, line)
+            zre.append(hexfloat(a))
+            zim.append(hexfloat(b))
+    want = O.points_julia_mpfr(zre, zim, hexfloat(jr.to_fraction()), hexfloat(ji.to_fraction()),
+                               depth, 2 * prec, fractal=fractal, threads=8)
+    diff = req.counts.ravel() != want
+    print(f"julia formula {fractal}: {int(diff.sum())}/{diff.size} differ from MPFR at "
+          f"{2 * prec} bits")
+    assert diff.mean() <= 0.001 or diff.sum() <= 2
+    assert len(np.unique(want)) > 10
+
+
 def test_serve_admission_by_footprint():
     reqs = [view_request("p_c4_600", W=160, H=120) for _ in range(5)]
     dev, host = footprint(reqs[0])
