@@ -236,6 +236,19 @@ int mdzgpu_render_perturb(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
                           const mdzgpu_mpval* width, int64_t precision,
                           int32_t limbs, int32_t* counts, float* mag2,
                           mdzgpu_stats* st);
+/* Julia family under perturbation (f->family = MDZ_FAMILY_JULIA; MDZ's
+ * Julia loop, src/fractal.c:55-59 and :78-88: z0 = the pixel, c = the
+ * constant).  Two reference orbits: the view's, from the centre, which the
+ * pixels start on with their offset as delta (no dc term), and the
+ * critical one, from 0, which every rebase goes to.  No counterpart in the
+ * reference (MDZ iterates every pixel in MPFR). */
+int mdzgpu_render_perturb_julia(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
+                                const mdzgpu_mpval* cx, const mdzgpu_mpval* cy,
+                                const mdzgpu_mpval* width,
+                                const mdzgpu_mpval* julia_re,
+                                const mdzgpu_mpval* julia_im, int64_t precision,
+                                int32_t limbs, int32_t* counts, float* mag2,
+                                mdzgpu_stats* st);
 int mdzgpu_render_perturb_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
                                  const mdzgpu_mpval* cx,
                                  const mdzgpu_mpval* cy,

@@ -135,18 +135,24 @@ class Renderer:
     def render_perturb(self, W: int, H: int, depth: int, cx: MpVal, cy: MpVal, width: MpVal,
                        precision: int, limbs: int = 0, want_mag: bool = False,
                        out: np.ndarray | None = None, mag: np.ndarray | None = None,
-                       fractal: int = 0):
-        f = Frame(W, H, 0, fractal, depth)
+                       fractal: int = 0, julia: tuple | None = None):
+        """julia = (re, im) as MpVal: the Julia family (z0 = pixel)."""
+        f = Frame(W, H, 1 if julia else 0, fractal, depth)
         if out is None:
             out = np.empty((H, W), np.int32)
         if want_mag and mag is None:
             mag = np.empty((H, W), np.float32)
         st = Stats()
-        items = [v.struct() for v in (cx, cy, width)]
-        _check(self.lib.mdzgpu_render_perturb(self.ctx, C.byref(f),
-                                              *[C.byref(s) for s, _ in items], precision, limbs,
-                                              _ptr(out), _ptr(mag if want_mag else None),
-                                              C.byref(st)))
+        items = [v.struct() for v in (cx, cy, width) + (tuple(julia) if julia else ())]
+        refs = [C.byref(s) for s, _ in items]
+        if julia:
+            _check(self.lib.mdzgpu_render_perturb_julia(
+                self.ctx, C.byref(f), *refs, precision, limbs, _ptr(out),
+                _ptr(mag if want_mag else None), C.byref(st)))
+        else:
+            _check(self.lib.mdzgpu_render_perturb(self.ctx, C.byref(f), *refs, precision, limbs,
+                                                  _ptr(out), _ptr(mag if want_mag else None),
+                                                  C.byref(st)))
         return out, (mag if want_mag else None), st.as_dict()
 
     def render_perturb_device(self, W, H, depth, cx, cy, width, precision, d_out_ptr: int,

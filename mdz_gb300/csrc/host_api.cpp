@@ -688,10 +688,12 @@ static int perturb_steps(mdzgpu_ctx* ctx, const PerturbLaunch& p, size_t n,
     }
 }
 
+// jre / jim: the Julia constant (Julia family), else null.
 static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,
                           const mdzgpu_mpval* cy, const mdzgpu_mpval* width, int64_t precision,
                           int32_t limbs, int32_t* d_out, float* d_mag, int32_t* h_out,
-                          float* h_mag, mdzgpu_stats* st)
+                          float* h_mag, mdzgpu_stats* st, const mdzgpu_mpval* jre = nullptr,
+                          const mdzgpu_mpval* jim = nullptr)
 {
     const double t0 = now_ms();
     if (!ctx) {
@@ -701,10 +703,16 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     int rc = validate_frame(f);
     if (rc)
         return rc;
-    if (f->family != MDZ_FAMILY_MANDEL || f->fractal == MDZ_VARIANT) {
-        set_error("perturbation: the Mandelbrot family with the Mandelbrot, burning ship or "
-                  "celtic formula");
+    const bool julia = f->family == MDZ_FAMILY_JULIA;
+    if ((f->family != MDZ_FAMILY_MANDEL && !julia) || f->fractal == MDZ_VARIANT) {
+        set_error("perturbation: the Mandelbrot or Julia family with the Mandelbrot, burning "
+                  "ship or celtic formula");
         return MDZGPU_ERR_UNSUPPORTED;
+    }
+    if (julia != (jre && jim)) {
+        set_error(julia ? "perturbation: the Julia family needs its constant"
+                        : "perturbation: a Julia constant outside the Julia family");
+        return MDZGPU_ERR_ARG;
     }
     MDZ_CUDA_TRY(cudaSetDevice(ctx->device));
     const int L = limbs > 0 ? limbs : mdzgpu_perturb_limbs(precision);
@@ -712,7 +720,8 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         set_error("perturbation: %d orbit limbs outside [5, %d]", L, orbit_max_limbs());
         return MDZGPU_ERR_UNSUPPORTED;
     }
-    std::vector<int> dig(2 * (size_t)L);
+    // digits: the centre, then (Julia) the constant
+    std::vector<int> dig((julia ? 4 : 2) * (size_t)L);
     if (digits28_from_mpval(cx, L, dig.data()) || digits28_from_mpval(cy, L, dig.data() + L)) {
         set_error("perturbation: centre outside the fixed-point range");
         return MDZGPU_ERR_RANGE;
@@ -721,15 +730,24 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         set_error("perturbation: centre must satisfy |cx|, |cy| < 4");
         return MDZGPU_ERR_RANGE;
     }
+    if (julia && (digits28_from_mpval(jre, L, dig.data() + 2 * L)
+                  || digits28_from_mpval(jim, L, dig.data() + 3 * L)
+                  || abs(dig[3 * L - 1]) >= 4 || abs(dig[4 * L - 1]) >= 4)) {
+        set_error("perturbation: the Julia constant must satisfy |re|, |im| < 4");
+        return MDZGPU_ERR_RANGE;
+    }
     double hs_m = 0.0;
     int hs_e = 0;
     if ((rc = half_spacing(width, f->width, &hs_m, &hs_e)))
         return rc;
     const size_t n = (size_t)f->width * f->height;
-    const OrbitLayout ol = orbit_layout((size_t)f->depth + 2, L);
+    // Julia: the view orbit V in entries [0, q0), the critical orbit Q from
+    // q0 (a multiple of 1024, so both bit masks start on a word)
+    const size_t q0 = julia ? ((size_t)f->depth + 2 + 1023) / 1024 * 1024 : 0;
+    const OrbitLayout ol = orbit_layout(q0 + (size_t)f->depth + 2, L);
     const size_t off_zd = ol.zd, off_ze = ol.ze, off_dd = ol.dd, off_de = ol.de;
-    const size_t off_len = ol.len, off_dig = ol.dig, off_reb = ol.reb, off_raw = ol.raw;
-    const size_t orbit_bytes = ol.bytes;
+    const size_t off_len = ol.len, off_dig = ol.bytes, off_reb = ol.reb, off_raw = ol.raw;
+    const size_t orbit_bytes = ol.bytes + dig.size() * sizeof(int);
     if ((rc = ctx->orbit.ensure(orbit_bytes)) || (rc = ctx->sync.ensure(sizeof(FrameSync))))
         return rc;
     if (!d_out) {
@@ -766,6 +784,26 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.fm = (double*)(ob + ol.fm);
     o.fe = (int*)(ob + ol.fe);
     o.axis = (unsigned*)(ob + ol.axis);
+    OrbitLaunch oq = o;   // Julia: the critical orbit
+    if (julia) {
+        // V: Z_0 = centre, constant c_J; Q: Z_0 = 0, constant c_J
+        o.z0_re = o.c_re;
+        o.z0_im = o.c_im;
+        o.c_re = o.c_re + 2 * L;
+        o.c_im = o.c_re + L;
+        oq.c_re = o.c_re;
+        oq.c_im = o.c_im;
+        oq.zq = o.zq + q0;
+        oq.zd = o.zd + q0;
+        oq.ze = o.ze + q0;
+        oq.dd = o.dd + q0;
+        oq.de = o.de + q0;
+        oq.fm = o.fm + q0;
+        oq.fe = o.fe + q0;
+        oq.tiny = o.tiny + q0 / 32;
+        oq.axis = o.axis + q0 / 32;
+        oq.out_len = o.out_len + 16;   // beside V's length, in the zeroed progress block
+    }
     int64_t h2d_extra = 0;
     cudaEvent_t evo;
     MDZ_CUDA_TRY(cudaEventCreate(&evo));
@@ -785,8 +823,9 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     const char* menv = getenv("MDZGPU_PERTURB");
     const char* fenv = getenv("MDZGPU_FUSED");
     const bool fused = ((fenv && fenv[0] == '1') || (menv && !strcmp(menv, "fused")))
-                       && f->fractal == MDZ_MANDELBROT;
-    const bool stepped = !fused && !(menv && !strcmp(menv, "frame"));
+                       && f->fractal == MDZ_MANDELBROT && !julia;
+    // Julia: both orbits first (every rebase may need any entry of Q)
+    const bool stepped = !fused && !julia && !(menv && !strcmp(menv, "frame"));
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
     if (stepped) {
         MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->stream));   // inputs in place
@@ -799,7 +838,8 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->side));      // orbit complete
     } else {
         if (!fused) {
-            if ((rc = launch_orbit(o, ctx->stream))) {
+            if ((rc = launch_orbit(o, ctx->stream))
+                || (julia && (rc = launch_orbit(oq, ctx->stream)))) {
                 cudaEventDestroy(evo);
                 return rc;
             }
@@ -825,6 +865,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.fm = o.fm;
     p.fe = o.fe;
     p.axis = o.axis;
+    if (julia) {
+        p.q0 = (int)q0;
+        p.q_len = oq.out_len;
+    }
     p.out = d_out;
     p.mag = d_mag;
     p.sync = (FrameSync*)ctx->sync.ptr;
@@ -880,9 +924,13 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     {
         const int w = perturb_mp_words((long)precision);
         std::vector<uint32_t> tab((size_t)(f->width + f->height + 2) * w, 0);
-        if ((rc = perturb_tables(cx, cy, hs_m, hs_e, f->width, f->height, w, tab))) {
+        if ((rc = perturb_tables(cx, cy, hs_m, hs_e, f->width, f->height, w, tab))
+            || (julia
+                && (fx_from_mpval(jre, w, tab.data() + (size_t)(f->width + f->height) * w)
+                    || fx_from_mpval(jim, w, tab.data() + (size_t)(f->width + f->height + 1) * w)))) {
+            set_error("perturbation: coordinates outside the fixed-point range");
             cudaEventDestroy(evo);
-            return rc;
+            return rc ? rc : MDZGPU_ERR_RANGE;
         }
         if ((rc = ctx->coords.ensure(tab.size() * 4))) {
             cudaEventDestroy(evo);
@@ -897,7 +945,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         q.H = f->height;
         q.row0 = 0;
         q.nrows = f->height;
-        q.family = MDZ_FAMILY_MANDEL;
+        q.family = julia ? MDZ_FAMILY_JULIA : MDZ_FAMILY_MANDEL;
         q.fractal = f->fractal;
         q.depth = (uint32_t)f->depth;
         q.words = w;
@@ -1055,6 +1103,20 @@ int mdzgpu_render_perturb(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     }
     return perturb_common(ctx, f, cx, cy, width, precision, limbs, nullptr, nullptr, counts, mag2,
                           st);
+}
+
+int mdzgpu_render_perturb_julia(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_mpval* cx,
+                                const mdzgpu_mpval* cy, const mdzgpu_mpval* width,
+                                const mdzgpu_mpval* julia_re, const mdzgpu_mpval* julia_im,
+                                int64_t precision, int32_t limbs, int32_t* counts, float* mag2,
+                                mdzgpu_stats* st)
+{
+    if (!counts || !julia_re || !julia_im) {
+        set_error("null argument");
+        return MDZGPU_ERR_ARG;
+    }
+    return perturb_common(ctx, f, cx, cy, width, precision, limbs, nullptr, nullptr, counts, mag2,
+                          st, julia_re, julia_im);
 }
 
 int mdzgpu_render_perturb_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,

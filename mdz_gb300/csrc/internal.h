@@ -180,6 +180,10 @@ struct OrbitLaunch {
     double* fm = nullptr;
     int* fe = nullptr;
     unsigned* axis = nullptr;
+    // Julia family: Z_0 = (z0_re, z0_im) (the view centre) and c_re / c_im
+    // the Julia constant; null: Z_0 = 0 (then Z_1 = C)
+    const int* z0_re = nullptr;
+    const int* z0_im = nullptr;
 };
 int launch_orbit(const OrbitLaunch& p, cudaStream_t s);
 int orbit_max_limbs();
@@ -187,6 +191,12 @@ int orbit_max_limbs();
 struct PerturbLaunch {
     int W, H, row0, nrows;
     uint32_t depth;
+    // Julia family (q_len non-null): entries [0, *orbit_len) are the view
+    // orbit V (V_0 = centre, no dc term: a pixel starts at V_0 with its
+    // offset as delta); entries [q0, q0 + *q_len) the critical orbit Q
+    // (Q_0 = 0), which every rebase and the end of either orbit go to
+    int q0 = 0;
+    const int* q_len = nullptr;
     double hs_m;            // half pixel spacing = hs_m * 2^hs_e, <= 40 bits
     int hs_e;
     const float4* zq;

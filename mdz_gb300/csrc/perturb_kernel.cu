@@ -129,14 +129,21 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
     const int part = warp & 1;   // 0: real, 1: imaginary
     const int half = warp >> 1;  // which half of each column's terms
     const int L = p.limbs;
+    const bool from_z0 = p.z0_re != nullptr;   // Julia: Z_0 given, k starts at 0
     for (int j = threadIdx.x; j < L; j += kOrbitThreads) {
         cc[0][j] = p.c_re[j];
         cc[1][j] = p.c_im[j];
-        z[j] = make_int2(p.c_re[j], p.c_im[j]);
-        p.digits[j] = 0;                    // Z_0 = 0
-        p.digits[L + j] = 0;
-        p.digits[2 * L + j] = p.c_re[j];    // Z_1 = C
-        p.digits[3 * L + j] = p.c_im[j];
+        if (from_z0) {
+            z[j] = make_int2(p.z0_re[j], p.z0_im[j]);
+            p.digits[j] = p.z0_re[j];
+            p.digits[L + j] = p.z0_im[j];
+        } else {
+            z[j] = make_int2(p.c_re[j], p.c_im[j]);
+            p.digits[j] = 0;                    // Z_0 = 0
+            p.digits[L + j] = 0;
+            p.digits[2 * L + j] = p.c_re[j];    // Z_1 = C
+            p.digits[3 * L + j] = p.c_im[j];
+        }
     }
     const int cbase = L - 4;       // lowest column computed (3 guard columns)
     const int ctop = 2 * L - 2;    // highest column
@@ -144,7 +151,7 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
     const int* cpart = cc[part];
     const bool ship = p.fractal == MDZ_BURNING_SHIP;
     const bool celtic = p.fractal == MDZ_GENERALIZED_CELTIC;
-    int k = 1;
+    int k = from_z0 ? 0 : 1;
     for (;; ++k) {
         if (prog && (k & 31) == 0) {
             __threadfence();  // this thread's digits of Z_0..Z_k
@@ -1119,7 +1126,7 @@ __device__ __forceinline__ OrbitSnap orbit_snapshot(const PerturbLaunch& p)
 // continues on the general path, so the operations are the same whether a
 // pixel runs in blocks or not, and a pixel resumed at any iteration gets
 // bit-identical results.
-template <class T, int MODE, int FR = MDZ_MANDELBROT>
+template <class T, int MODE, int FR = MDZ_MANDELBROT, bool JU = false>
 __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, double dcm_i,
                            int dce, uint32_t wz_last, uint32_t& count, BlockOrbitView* view,
                            OrbitSnap snap = OrbitSnap{0, 0})
@@ -1130,6 +1137,12 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
     // entries 0..avail-1 readable; K = orbit length (unknown while streaming)
     int K = MODE == kOrbitComplete ? *p.orbit_len : (MODE == kOrbitSnapshot ? snap.K : 0x7fffffff);
     int avail = MODE == kOrbitSnapshot ? snap.avail : K;
+    // Julia: K ends the orbit segment the pixel is on (V, or Q from q0)
+    const int q0 = JU ? p.q0 : 0;
+    if (JU) {
+        K = m < q0 ? *p.orbit_len : q0 + *p.q_len;
+        avail = K;
+    }
     if (MODE == kOrbitWait && !wait_orbit(p, view, m, avail, K))
         return -1;
     if (MODE == kOrbitSnapshot && m >= avail)
@@ -1292,7 +1305,9 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                     rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, rebase_lost, false);
                     if (kTrack)
                         fold_rebase_err<T>(p, m, st, e0);
-                    m = 0;
+                    m = q0;
+                    if (JU)
+                        K = avail = q0 + *p.q_len;
                     Zx = (T)0;
                     Zy = (T)0;
                     fs = (T)1;
@@ -1376,7 +1391,9 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
             if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, rebase_lost, true)) {
                 if (kTrack)
                     fold_rebase_err<T>(p, m, st, e0);
-                m = 0;
+                m = q0;
+                if (JU)
+                    K = avail = q0 + *p.q_len;
                 Zx = (T)0;
                 Zy = (T)0;
                 fs = (T)1;
@@ -1443,16 +1460,21 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
 // below `avail` are finished; a pixel that needs entry m + 1 waits (bounded)
 // for the finisher, and learns the final length K once the producer is done.
 // A wait that gives up raises the error flag and leaves the count 0.
-template <class T, bool STREAM, int FR>
+template <class T, bool STREAM, int FR, bool JU = false>
 __device__ uint32_t perturb_pixel(const PerturbLaunch& p, double dcm_r, double dcm_i, int dce,
                                   float& mag_out, unsigned& rebases, float& lost,
                                   BlockOrbitView* view)
 {
     PixRun<T> r;
     pixel_start(r, dcm_r, dcm_i, dce, fold_ke<T>(p));
+    if (JU) {
+        // Julia: the offset is the first delta, at V_0; no dc in the steps
+        r.m = 0;
+        refresh_scale(r.st, (T)0, (T)0, dce);
+    }
     uint32_t count = 0;
-    const int done = perturb_run<T, STREAM ? kOrbitWait : kOrbitComplete, FR>(
-        p, r, dcm_r, dcm_i, dce, p.depth, count, view);
+    const int done = perturb_run<T, STREAM ? kOrbitWait : kOrbitComplete, FR, JU>(
+        p, r, JU ? 0.0 : dcm_r, JU ? 0.0 : dcm_i, dce, p.depth, count, view);
     mag_out = r.mag;
     rebases += r.rebases;
     lost += r.lost;
@@ -1471,7 +1493,7 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 // (FP64) walks the list of pixels the previous pass flagged, in warp-sized
 // chunks.  Each pass appends the pixels it could not finish precisely to
 // p.flag_out; pixel-iterations are counted only for pixels it finalises.
-template <class T, bool WANT_MAG, bool LIST, bool STREAM, int FR>
+template <class T, bool WANT_MAG, bool LIST, bool STREAM, int FR, bool JU = false>
 __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
 {
     __shared__ BlockOrbitView view;
@@ -1523,7 +1545,7 @@ __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
             const double dcm_i = (double)(p.H - 2 * line) * p.hs_m;
             float mag = 0.f, lost = 0.f;
             const uint32_t n =
-                perturb_pixel<T, STREAM, FR>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost, &view);
+                perturb_pixel<T, STREAM, FR, JU>(p, dcm_r, dcm_i, p.hs_e, mag, reb, lost, &view);
             const size_t o = (size_t)lrow * p.W + ix;
             p.out[o] = (int32_t)n;
             if (WANT_MAG)
@@ -1546,10 +1568,10 @@ __device__ __forceinline__ void pixel_tiles(const PerturbLaunch& p)
     }
 }
 
-template <class T, bool WANT_MAG, bool LIST, int FR>
+template <class T, bool WANT_MAG, bool LIST, int FR, bool JU>
 __global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
 {
-    pixel_tiles<T, WANT_MAG, LIST, false, FR>(p);
+    pixel_tiles<T, WANT_MAG, LIST, false, FR, JU>(p);
     if (p.done.count) {
         const unsigned long long total = LIST ? (*p.list_in_count + 31u) / 32u : 0u;
         done_signal(p.done,
@@ -2002,25 +2024,25 @@ int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
     return MDZGPU_OK;
 }
 
-template <class T, bool WANT_MAG, bool LIST, int FR>
+template <class T, bool WANT_MAG, bool LIST, int FR, bool JU = false>
 int pass_blocks_per_sm(int* out)
 {
     static int bps = 0;
     if (!bps) {
         int b = 0;
         MDZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &b, perturb_kernel<T, WANT_MAG, LIST, FR>, 256, 0));
+            &b, perturb_kernel<T, WANT_MAG, LIST, FR, JU>, 256, 0));
         bps = b < 1 ? 1 : b;
     }
     *out = bps;
     return MDZGPU_OK;
 }
 
-template <class T, bool WANT_MAG, bool LIST, int FR>
+template <class T, bool WANT_MAG, bool LIST, int FR, bool JU>
 int launch_pass_fr(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
 {
     int bps = 1;
-    if (int rc = pass_blocks_per_sm<T, WANT_MAG, LIST, FR>(&bps))
+    if (int rc = pass_blocks_per_sm<T, WANT_MAG, LIST, FR, JU>(&bps))
         return rc;
     long grid = (long)ctx->num_sms * bps;
     const long blocks_needed = (work_items + 7) / 8;
@@ -2028,19 +2050,26 @@ int launch_pass_fr(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long
         grid = blocks_needed;
     if (grid < 1)
         grid = 1;
-    perturb_kernel<T, WANT_MAG, LIST, FR><<<(unsigned)grid, 256, 0, s>>>(p);
+    perturb_kernel<T, WANT_MAG, LIST, FR, JU><<<(unsigned)grid, 256, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
     return MDZGPU_OK;
+}
+
+template <class T, bool WANT_MAG, bool LIST, bool JU>
+int launch_pass_ju(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
+{
+    if (p.fractal == MDZ_BURNING_SHIP)
+        return launch_pass_fr<T, WANT_MAG, LIST, 1, JU>(ctx, p, s, work_items);
+    if (p.fractal == MDZ_GENERALIZED_CELTIC)
+        return launch_pass_fr<T, WANT_MAG, LIST, 2, JU>(ctx, p, s, work_items);
+    return launch_pass_fr<T, WANT_MAG, LIST, 0, JU>(ctx, p, s, work_items);
 }
 
 template <class T, bool WANT_MAG, bool LIST>
 int launch_pass(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
 {
-    if (p.fractal == MDZ_BURNING_SHIP)
-        return launch_pass_fr<T, WANT_MAG, LIST, 1>(ctx, p, s, work_items);
-    if (p.fractal == MDZ_GENERALIZED_CELTIC)
-        return launch_pass_fr<T, WANT_MAG, LIST, 2>(ctx, p, s, work_items);
-    return launch_pass_fr<T, WANT_MAG, LIST, 0>(ctx, p, s, work_items);
+    return p.q_len ? launch_pass_ju<T, WANT_MAG, LIST, true>(ctx, p, s, work_items)
+                   : launch_pass_ju<T, WANT_MAG, LIST, false>(ctx, p, s, work_items);
 }
 
 template <int FR>
@@ -2055,6 +2084,14 @@ int preload_fr()
         rc = pass_blocks_per_sm<double, false, true, FR>(&b);
     if (!rc)
         rc = pass_blocks_per_sm<double, true, true, FR>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<float, false, false, FR, true>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<float, true, false, FR, true>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<double, false, true, FR, true>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<double, true, true, FR, true>(&b);
     cudaFuncAttributes a;
     if (!rc && (cudaFuncGetAttributes(&a, perturb_step_kernel<false, FR>) != cudaSuccess
                 || cudaFuncGetAttributes(&a, perturb_step_kernel<true, FR>) != cudaSuccess

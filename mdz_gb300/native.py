@@ -100,6 +100,8 @@ _SIGS = {
                                 + [C.c_int64, C.c_int32, P, C.POINTER(Stats)]),
     "mdzgpu_render_perturb": (C.c_int, [P, C.POINTER(Frame)] + [C.POINTER(MpValStruct)] * 3
                               + [C.c_int64, C.c_int32, P, P, C.POINTER(Stats)]),
+    "mdzgpu_render_perturb_julia": (C.c_int, [P, C.POINTER(Frame)] + [C.POINTER(MpValStruct)] * 5
+                                    + [C.c_int64, C.c_int32, P, P, C.POINTER(Stats)]),
     "mdzgpu_render_perturb_device": (C.c_int, [P, C.POINTER(Frame)]
                                      + [C.POINTER(MpValStruct)] * 3
                                      + [C.c_int64, C.c_int32, P, P, C.POINTER(Stats)]),

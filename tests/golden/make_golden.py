@@ -9,6 +9,7 @@ the reference sources exist; the GPU machine only reads the outputs).
   python tests/golden/make_golden.py centres   # serve_centres.json (serving stream centres)
   python tests/golden/make_golden.py colour    # colour.npz (reference palette_apply / AA)
   python tests/golden/make_golden.py perturb_fold  # perturb_fold.npz (ship / celtic, MPFR 2p)
+  python tests/golden/make_golden.py perturb_julia # perturb_julia.npz (Julia family, MPFR 2p)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -539,6 +540,72 @@ def make_perturb_fold() -> None:
     (GOLD / "perturb_fold_views.json").write_text(json.dumps(meta, indent=1))
 
 
+def julia_boundary_point(fr: int, jre: str, jim: str, a: tuple, b: tuple, bits: int,
+                         depth: int) -> tuple:
+    """A point of the Julia set's boundary by bisection on the segment a -> b
+    (a inside: never escapes within depth; b outside), at `bits` bits; the
+    constant (jre, jim) as exact hexadecimal strings."""
+    def escapes(z):
+        x, y = z
+        c = O.points_julia_mpfr([hexfloat(x)], [hexfloat(y)], jre, jim, depth, bits + 64,
+                                fractal=fr)
+        return int(c[0]) != 0
+    lo, hi = (Fraction(a[0]), Fraction(a[1])), (Fraction(b[0]), Fraction(b[1]))
+    assert not escapes(lo) and escapes(hi)
+    for _ in range(bits):
+        mid = ((lo[0] + hi[0]) / 2, (lo[1] + hi[1]) / 2)
+        if escapes(mid):
+            hi = mid
+        else:
+            lo = mid
+    return lo
+
+
+def make_perturb_julia() -> None:
+    """Julia-family frames (z0 = pixel, c fixed) for the perturbation with a
+    view orbit and a critical orbit: centres on the Julia sets' boundaries
+    (bisection at depth 10^4), scored against MPFR at 2p, with p and 3p
+    stored to classify each view as in make_perturb_fold."""
+    P = Fraction(2)
+    specs = [
+        ("j_basilica_40", 0, "-1", "0", (0, 0), (2, "0.75"), 48, 36, 3000, P ** -40, 104),
+        ("j_basilica_200", 0, "-1", "0", (0, 0), (2, "0.75"), 48, 36, 6000, P ** -200, 264),
+        ("j_rabbit_600", 0, "-0.122561166876654", "0.744861766619744", (0, 0), ("1.5", "1"),
+         32, 24, 8000, P ** -600, 664),
+        ("j_ship_100", 1, "-0.5", "-0.5", (0, 0), (0, 2), 48, 36, 4000, P ** -100, 164),
+        ("j_celtic_150", 2, "-1", "0.1", (0, 0), (2, "0.125"), 48, 36, 4000, P ** -150, 214),
+    ]
+    out, meta = {}, {}
+    for name, fr, jre, jim, a, b, W, H, depth, width, prec in specs:
+        t0 = time.time()
+        jr = MpVal.from_fraction(Fraction(jre), prec).to_fraction()
+        ji = MpVal.from_fraction(Fraction(jim), prec).to_fraction()
+        cx, cy = julia_boundary_point(fr, hexfloat(jr), hexfloat(ji), a, b, prec, 10000)
+        cx = MpVal.from_fraction(cx, prec).to_fraction()
+        cy = MpVal.from_fraction(cy, prec).to_fraction()
+        width = MpVal.from_fraction(width, prec).to_fraction()
+        zre, zim = [], []
+        for ln in range(H):
+            for ix in range(W):
+                x, y = perturb_c(cx, cy, width, W, H, ix, ln)
+                zre.append(hexfloat(x))
+                zim.append(hexfloat(y))
+        got = [O.points_julia_mpfr(zre, zim, hexfloat(jr), hexfloat(ji), depth, q, fractal=fr,
+                                   threads=THREADS) for q in (prec, 2 * prec, 3 * prec)]
+        agree = float(((got[0] == got[1]) & (got[1] == got[2])).mean())
+        out[name] = got[1].reshape(H, W).astype(np.int32)
+        out[name + "__p"] = got[0].reshape(H, W).astype(np.int32)
+        out[name + "__3p"] = got[2].reshape(H, W).astype(np.int32)
+        meta[name] = dict(fractal=fr, julia_re=hexfloat(jr), julia_im=hexfloat(ji),
+                          cx=hexfloat(cx), cy=hexfloat(cy), width=hexfloat(width), W=W, H=H,
+                          depth=depth, prec=prec, oracle_prec=2 * prec,
+                          kind="resolved" if agree >= 0.99 else "chaotic")
+        print(f"{name}: {time.time() - t0:.1f}s distinct counts {len(np.unique(got[1]))} "
+              f"interior {(got[1] == 0).mean():.2f} p = 2p = 3p on {agree:.4f}", flush=True)
+    np.savez_compressed(GOLD / "perturb_julia.npz", **out)
+    (GOLD / "perturb_julia_views.json").write_text(json.dumps(meta, indent=1))
+
+
 def parse_num(s):
     from mdz_gb300.mpval import parse_number
     return parse_number(s)
@@ -564,7 +631,7 @@ def main(argv: list[str]) -> None:
     for w in what:
         {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
          "perturb": make_perturb, "centres": make_centres, "colour": make_colour,
-         "perturb_fold": make_perturb_fold}[w]()
+         "perturb_fold": make_perturb_fold, "perturb_julia": make_perturb_julia}[w]()
 
 
 if __name__ == "__main__":
