@@ -2,11 +2,14 @@
 
     python -m mdz_gb300.cases c2 [--frame 480x270] [--repeat 1]
     python -m mdz_gb300.cases c3 | c4 | serve [--requests 4]
+    python -m mdz_gb300.cases ship [--frame 480x270]
 
 c1/c2: FP64 kernel (MDZ's double path) on the views' rectangles (c2 without
 supersampling unless --aa); c3: the multi-limb kernel at 256 bits; c4: the
 perturbation frame (orbit + FP32 pixels + escalation passes); serve: the
-first requests of the seeded serving stream through the serving engine.
+first requests of the seeded serving stream through the serving engine;
+ship: the burning-ship perturbation on the 2^-300 view of the folded-formula
+fixtures (tests/golden/perturb_fold_views.json, f_ship_a300).
 --frame keeps the view's pixel spacing and crops around its centre.
 Prints one JSON line of the call's statistics per repeat.
 """
@@ -37,7 +40,7 @@ def view(name: str, frame: str | None, aa: bool) -> View:
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["c1", "c2", "c3", "c4", "serve"])
+    ap.add_argument("case", choices=["c1", "c2", "c3", "c4", "serve", "ship"])
     ap.add_argument("--frame", default=None)
     ap.add_argument("--aa", action="store_true")
     ap.add_argument("--repeat", type=int, default=1)
@@ -54,6 +57,19 @@ def main(argv=None) -> None:
                 sts = [srv.wait(i) for i in ids]
                 print(json.dumps({"requests": len(sts), "states": [s["state"] for s in sts],
                                   "stats": srv.stats()}), flush=True)
+        return
+    if a.case == "ship":
+        m = json.loads((Path(__file__).resolve().parents[1] / "tests" / "golden" /
+                        "perturb_fold_views.json").read_text())["f_ship_a300"]
+        W, H = (int(x) for x in (a.frame or "480x270").lower().split("x"))
+        prec = m["prec"]
+        vals = [MpVal.from_fraction(parse_number(m[k]), prec) for k in ("cx", "cy")]
+        w = MpVal.from_fraction(parse_number(m["width"]) * Fraction(W, m["W"]), prec)
+        with Renderer(0) as r:
+            for _ in range(a.repeat):
+                _, _, st = r.render_perturb(W, H, m["depth"], vals[0], vals[1], w, prec,
+                                            fractal=m["fractal"])
+                print(json.dumps(st), flush=True)
         return
     v = view(a.case, a.frame, a.aa)
     with Renderer(0) as r:
