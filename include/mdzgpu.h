@@ -218,10 +218,13 @@ int mdzgpu_colour_device(mdzgpu_ctx* ctx, const int32_t* d_counts,
 int32_t mdzgpu_mp_max_words(void);
 
 /* Perturbation path (new method; the reference has none).  Renders the
- * Mandelbrot family with the Mandelbrot, burning ship or generalized celtic
- * formula (f->fractal; the folded formulas take |c + d| - |c| from the
- * orbit's exact side of the fold, and an exact FP64 step wherever a pixel
- * can cross it) around the centre (cx, cy) with real-axis
+ * Mandelbrot family with the Mandelbrot, burning ship, generalized celtic
+ * or variant formula (f->fractal; the folded formulas take |c + d| - |c|
+ * from the orbit's exact side of the fold, and an exact FP64 step wherever
+ * a pixel can cross it; the variant, whose fold applies on odd iterations
+ * only, keeps two orbits, folding at odd and at even steps, and rebases
+ * onto the one that matches the pixel's iteration parity) around the
+ * centre (cx, cy) with real-axis
  * `width`: pixel (ix, line) is c = (cx + (2 ix - W) hs, cy + (H - 2 line) hs)
  * where hs = width / (2 W) rounded to 40 significant bits (exactly the value
  * mdzgpu_perturb_spacing returns; this is MDZ's centre/size geometry,

@@ -704,9 +704,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     if (rc)
         return rc;
     const bool julia = f->family == MDZ_FAMILY_JULIA;
-    if ((f->family != MDZ_FAMILY_MANDEL && !julia) || f->fractal == MDZ_VARIANT) {
-        set_error("perturbation: the Mandelbrot or Julia family with the Mandelbrot, burning "
-                  "ship or celtic formula");
+    const bool variant = f->fractal == MDZ_VARIANT;
+    if ((f->family != MDZ_FAMILY_MANDEL && !julia) || (julia && variant)) {
+        set_error("perturbation: the Mandelbrot family with any formula, or the Julia family "
+                  "with the Mandelbrot, burning ship or celtic formula");
         return MDZGPU_ERR_UNSUPPORTED;
     }
     if (julia != (jre && jim)) {
@@ -742,8 +743,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         return rc;
     const size_t n = (size_t)f->width * f->height;
     // Julia: the view orbit V in entries [0, q0), the critical orbit Q from
-    // q0 (a multiple of 1024, so both bit masks start on a word)
-    const size_t q0 = julia ? ((size_t)f->depth + 2 + 1023) / 1024 * 1024 : 0;
+    // q0 (a multiple of 1024, so both bit masks start on a word); the
+    // hybrid: the orbits that fold at odd / even steps
+    const bool two = julia || variant;
+    const size_t q0 = two ? ((size_t)f->depth + 2 + 1023) / 1024 * 1024 : 0;
     const OrbitLayout ol = orbit_layout(q0 + (size_t)f->depth + 2, L);
     const size_t off_zd = ol.zd, off_ze = ol.ze, off_dd = ol.dd, off_de = ol.de;
     const size_t off_len = ol.len, off_dig = ol.bytes, off_reb = ol.reb, off_raw = ol.raw;
@@ -784,15 +787,20 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.fm = (double*)(ob + ol.fm);
     o.fe = (int*)(ob + ol.fe);
     o.axis = (unsigned*)(ob + ol.axis);
-    OrbitLaunch oq = o;   // Julia: the critical orbit
-    if (julia) {
-        // V: Z_0 = centre, constant c_J; Q: Z_0 = 0, constant c_J
-        o.z0_re = o.c_re;
-        o.z0_im = o.c_im;
-        o.c_re = o.c_re + 2 * L;
-        o.c_im = o.c_re + L;
-        oq.c_re = o.c_re;
-        oq.c_im = o.c_im;
+    OrbitLaunch oq = o;   // Julia: the critical orbit; hybrid: the even-step one
+    if (two) {
+        if (julia) {
+            // V: Z_0 = centre, constant c_J; Q: Z_0 = 0, constant c_J
+            o.z0_re = o.c_re;
+            o.z0_im = o.c_im;
+            o.c_re = o.c_re + 2 * L;
+            o.c_im = o.c_re + L;
+            oq.c_re = o.c_re;
+            oq.c_im = o.c_im;
+        } else {
+            o.fold_parity = 1;
+            oq.fold_parity = 0;
+        }
         oq.zq = o.zq + q0;
         oq.zd = o.zd + q0;
         oq.ze = o.ze + q0;
@@ -823,9 +831,9 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     const char* menv = getenv("MDZGPU_PERTURB");
     const char* fenv = getenv("MDZGPU_FUSED");
     const bool fused = ((fenv && fenv[0] == '1') || (menv && !strcmp(menv, "fused")))
-                       && f->fractal == MDZ_MANDELBROT && !julia;
-    // Julia: both orbits first (every rebase may need any entry of Q)
-    const bool stepped = !fused && !julia && !(menv && !strcmp(menv, "frame"));
+                       && f->fractal == MDZ_MANDELBROT && !two;
+    // two orbits: both first (every rebase may need any entry of either)
+    const bool stepped = !fused && !two && !(menv && !strcmp(menv, "frame"));
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
     if (stepped) {
         MDZ_CUDA_TRY(cudaEventRecord(evo, ctx->stream));   // inputs in place
@@ -839,7 +847,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     } else {
         if (!fused) {
             if ((rc = launch_orbit(o, ctx->stream))
-                || (julia && (rc = launch_orbit(oq, ctx->stream)))) {
+                || (two && (rc = launch_orbit(oq, ctx->stream)))) {
                 cudaEventDestroy(evo);
                 return rc;
             }
@@ -865,9 +873,10 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.fm = o.fm;
     p.fe = o.fe;
     p.axis = o.axis;
-    if (julia) {
+    if (two) {
         p.q0 = (int)q0;
         p.q_len = oq.out_len;
+        p.julia = julia;
     }
     p.out = d_out;
     p.mag = d_mag;

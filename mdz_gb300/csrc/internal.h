@@ -184,6 +184,9 @@ struct OrbitLaunch {
     // the Julia constant; null: Z_0 = 0 (then Z_1 = C)
     const int* z0_re = nullptr;
     const int* z0_im = nullptr;
+    // MDZ_VARIANT (celtic fold on odd iterations, src/frac_variant.c:14-17):
+    // the step Z_k -> Z_{k+1} folds when k % 2 == fold_parity
+    int fold_parity = 1;
 };
 int launch_orbit(const OrbitLaunch& p, cudaStream_t s);
 int orbit_max_limbs();
@@ -194,9 +197,13 @@ struct PerturbLaunch {
     // Julia family (q_len non-null): entries [0, *orbit_len) are the view
     // orbit V (V_0 = centre, no dc term: a pixel starts at V_0 with its
     // offset as delta); entries [q0, q0 + *q_len) the critical orbit Q
-    // (Q_0 = 0), which every rebase and the end of either orbit go to
+    // (Q_0 = 0), which every rebase and the end of either orbit go to.
+    // MDZ_VARIANT: [0, *orbit_len) folds at odd steps, [q0, q0 + *q_len)
+    // at even steps; a rebase takes the one whose parity matches the
+    // pixel's iteration count.
     int q0 = 0;
     const int* q_len = nullptr;
+    bool julia = false;     // Julia family (z0 = pixel; see above)
     double hs_m;            // half pixel spacing = hs_m * 2^hs_e, <= 40 bits
     int hs_e;
     const float4* zq;

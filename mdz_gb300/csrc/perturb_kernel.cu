@@ -151,6 +151,7 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
     const int* cpart = cc[part];
     const bool ship = p.fractal == MDZ_BURNING_SHIP;
     const bool celtic = p.fractal == MDZ_GENERALIZED_CELTIC;
+    const bool variant = p.fractal == MDZ_VARIANT;
     int k = from_z0 ? 0 : 1;
     for (;; ++k) {
         if (prog && (k & 31) == 0) {
@@ -170,6 +171,8 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
             if (a * a + b * b > 4.0f || k >= p.max_k)
                 break;
         }
+        // celtic fold of this step (every step, or the variant's odd ones)
+        const bool fold_re = celtic || (variant && (k & 1) == p.fold_parity);
         // burning ship: Im' = 2 |Re| |Im| + Ci = sign(Re) sign(Im) 2 Re Im + Ci
         const int sxy = ship ? digits_sign_warp(z, L, false) * digits_sign_warp(z, L, true) : 1;
         long long v[3] = {0, 0, 0};
@@ -222,7 +225,7 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
             if (part == 1)
                 acc *= sxy;
             // celtic adds Cr after the fold (below)
-            if (!half && c >= L - 1 && !(celtic && part == 0))
+            if (!half && c >= L - 1 && !(fold_re && part == 0))
                 acc += cpart[c - (L - 1)];
             v[s] = acc;
         }
@@ -260,7 +263,7 @@ __device__ __noinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProg
             }
         };
         carry2();
-        if (celtic && part == 0) {
+        if (fold_re && part == 0) {
             // Re' = |Re^2 - Im^2| + Cr: the sign of the carried digits is
             // that of their most significant nonzero one
             int sg = 0;
@@ -361,7 +364,8 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
     const float fx = (float)vr, fy = (float)vi;
     // burning ship / celtic: the fold quantity F_k and its exact sign
     float fold_sign = 1.f;
-    if (p.fractal == MDZ_BURNING_SHIP || p.fractal == MDZ_GENERALIZED_CELTIC) {
+    if (p.fractal == MDZ_BURNING_SHIP || p.fractal == MDZ_GENERALIZED_CELTIC
+        || p.fractal == MDZ_VARIANT) {
         double fmv;
         int fev;
         if (p.fractal == MDZ_BURNING_SHIP) {
@@ -1071,6 +1075,9 @@ __device__ uint32_t fold_direct(double xr, double xi, double cr, double ci, uint
         if (FR == MDZ_BURNING_SHIP) {
             xr = a + cr;
             xi = 2.0 * fabs(b) + ci;
+        } else if (FR == MDZ_VARIANT && !(w & 1u)) {
+            xr = a + cr;   // the hybrid's even iterations are Mandelbrot's
+            xi = 2.0 * b + ci;
         } else {
             xr = fabs(a) + cr;
             xi = 2.0 * b + ci;
@@ -1137,12 +1144,25 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
     // entries 0..avail-1 readable; K = orbit length (unknown while streaming)
     int K = MODE == kOrbitComplete ? *p.orbit_len : (MODE == kOrbitSnapshot ? snap.K : 0x7fffffff);
     int avail = MODE == kOrbitSnapshot ? snap.avail : K;
-    // Julia: K ends the orbit segment the pixel is on (V, or Q from q0)
-    const int q0 = JU ? p.q0 : 0;
-    if (JU) {
+    // Julia and the hybrid carry two orbits: K ends the segment the pixel
+    // is on (the first, or the second from q0)
+    constexpr bool kVar = FR == MDZ_VARIANT;
+    constexpr bool kTwo = JU || kVar;
+    const int q0 = kTwo ? p.q0 : 0;
+    if (kTwo) {
         K = m < q0 ? *p.orbit_len : q0 + *p.q_len;
         avail = K;
     }
+    // where a rebase goes when iteration `next` steps from it: Julia: the
+    // critical orbit; the hybrid: the orbit that folds at the parity of
+    // `next` (the first folds at odd steps); else Z_0
+    auto rebase_to = [&](uint32_t next) -> int {
+        if (JU)
+            return q0;
+        if (kVar)
+            return (next & 1u) ? q0 : 0;
+        return 0;
+    };
     if (MODE == kOrbitWait && !wait_orbit(p, view, m, avail, K))
         return -1;
     if (MODE == kOrbitSnapshot && m >= avail)
@@ -1176,8 +1196,9 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
         // blocks: FP32 (the FP64 pass is the rare escalation path), no
         // slow step among the four (dz below the FP32 range needs one only
         // where Z_m is tiny)
-        if (FR != MDZ_MANDELBROT && sizeof(T) == 4 && (wz & 3u) == 1u && wz + 3u <= last
-            && m + 4 < avail && st.s == (T)0 && !st.force_slow && four_not_axis(p, m)) {
+        if (FR != MDZ_MANDELBROT && !kVar && sizeof(T) == 4 && (wz & 3u) == 1u
+            && wz + 3u <= last && m + 4 < avail && st.s == (T)0 && !st.force_slow
+            && four_not_axis(p, m)) {
             // folded formulas at deep zoom: z = Z_m in FP32 and no fold
             // within reach of dz among these entries, so the fold keeps
             // Z_m's side; same values as the general step with s = 0
@@ -1305,9 +1326,9 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                     rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, rebase_lost, false);
                     if (kTrack)
                         fold_rebase_err<T>(p, m, st, e0);
-                    m = q0;
-                    if (JU)
-                        K = avail = q0 + *p.q_len;
+                    m = rebase_to(wz);
+                    if (kTwo)
+                        K = avail = m ? q0 + *p.q_len : *p.orbit_len;
                     Zx = (T)0;
                     Zy = (T)0;
                     fs = (T)1;
@@ -1320,7 +1341,8 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
             }
             const bool careful = st.careful && (st.force_slow || z_tiny<T>(p, m, Zx, Zy));
             const T g = kTrack ? grow * magT : (T)0;
-            if (FR != MDZ_MANDELBROT) {
+            // the hybrid folds on odd iterations only
+            if (FR != MDZ_MANDELBROT && (!kVar || (wz & 1u))) {
                 // with dz below the T range (s = 0) a fold is out of reach
                 // unless the entry is marked: the same choice as the blocks
                 // (a lost estimate leaves only the rounding margin: the side
@@ -1391,9 +1413,9 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
             if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, rebase_lost, true)) {
                 if (kTrack)
                     fold_rebase_err<T>(p, m, st, e0);
-                m = q0;
-                if (JU)
-                    K = avail = q0 + *p.q_len;
+                m = rebase_to(wz + 1);
+                if (kTwo)
+                    K = avail = m ? q0 + *p.q_len : *p.orbit_len;
                 Zx = (T)0;
                 Zy = (T)0;
                 fs = (T)1;
@@ -2058,6 +2080,8 @@ int launch_pass_fr(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long
 template <class T, bool WANT_MAG, bool LIST, bool JU>
 int launch_pass_ju(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
 {
+    if (p.fractal == MDZ_VARIANT && !JU)
+        return launch_pass_fr<T, WANT_MAG, LIST, MDZ_VARIANT, false>(ctx, p, s, work_items);
     if (p.fractal == MDZ_BURNING_SHIP)
         return launch_pass_fr<T, WANT_MAG, LIST, 1, JU>(ctx, p, s, work_items);
     if (p.fractal == MDZ_GENERALIZED_CELTIC)
@@ -2068,7 +2092,7 @@ int launch_pass_ju(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long
 template <class T, bool WANT_MAG, bool LIST>
 int launch_pass(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, long work_items)
 {
-    return p.q_len ? launch_pass_ju<T, WANT_MAG, LIST, true>(ctx, p, s, work_items)
+    return p.julia ? launch_pass_ju<T, WANT_MAG, LIST, true>(ctx, p, s, work_items)
                    : launch_pass_ju<T, WANT_MAG, LIST, false>(ctx, p, s, work_items);
 }
 
@@ -2102,7 +2126,16 @@ int preload_fr()
 
 int preload_perturb_kernels()
 {
-    int rc = preload_fr<MDZ_MANDELBROT>();
+    int b = 0;
+    int rc = pass_blocks_per_sm<float, false, false, MDZ_VARIANT>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<float, true, false, MDZ_VARIANT>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<double, false, true, MDZ_VARIANT>(&b);
+    if (!rc)
+        rc = pass_blocks_per_sm<double, true, true, MDZ_VARIANT>(&b);
+    if (!rc)
+        rc = preload_fr<MDZ_MANDELBROT>();
     if (!rc)
         rc = preload_fr<MDZ_BURNING_SHIP>();
     if (!rc)

@@ -10,6 +10,7 @@ the reference sources exist; the GPU machine only reads the outputs).
   python tests/golden/make_golden.py colour    # colour.npz (reference palette_apply / AA)
   python tests/golden/make_golden.py perturb_fold  # perturb_fold.npz (ship / celtic, MPFR 2p)
   python tests/golden/make_golden.py perturb_julia # perturb_julia.npz (Julia family, MPFR 2p)
+  python tests/golden/make_golden.py perturb_variant  # perturb_variant.npz (hybrid, MPFR 2p)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -606,6 +607,63 @@ def make_perturb_julia() -> None:
     (GOLD / "perturb_julia_views.json").write_text(json.dumps(meta, indent=1))
 
 
+def variant_boundary_point(a: tuple, b: tuple, bits: int, depth: int) -> tuple:
+    """A boundary point of the variant formula's set by bisection on the
+    segment a -> b of the c plane (a: never escapes within depth; b escapes)."""
+    def escapes(z):
+        c, _ = O.points_mpfr([hexfloat(z[0])], [hexfloat(z[1])], depth, bits + 64, fractal=3)
+        return int(c[0]) != 0
+    lo, hi = (Fraction(a[0]), Fraction(a[1])), (Fraction(b[0]), Fraction(b[1]))
+    assert not escapes(lo) and escapes(hi)
+    for _ in range(bits):
+        mid = ((lo[0] + hi[0]) / 2, (lo[1] + hi[1]) / 2)
+        if escapes(mid):
+            hi = mid
+        else:
+            lo = mid
+    return lo
+
+
+def make_perturb_variant() -> None:
+    """MDZ's variant (mandel/celtic hybrid: the celtic fold on odd
+    iterations) under perturbation: frames around boundary points of its set
+    (bisection at depth 10^4), counts by MPFR at p, 2p and 3p bits,
+    classified as in make_perturb_fold."""
+    P = Fraction(2)
+    specs = [
+        ("v_a_50", ("-0.5", "0.5"), ("0.25", "0.5"), 48, 36, 12000, P ** -50, 114),
+        ("v_a_250", ("-0.5", "0.5"), ("0.25", "0.5"), 48, 36, 12000, P ** -250, 314),
+        ("v_b_120", ("-0.25", "0.25"), ("-0.75", "0.125"), 48, 36, 12000, P ** -120, 184),
+        ("v_b_500", ("-0.25", "0.25"), ("-0.75", "0.125"), 32, 24, 12000, P ** -500, 564),
+    ]
+    out, meta = {}, {}
+    for name, a, b, W, H, depth, width, prec in specs:
+        t0 = time.time()
+        cx, cy = variant_boundary_point(a, b, prec, 10000)
+        cx = MpVal.from_fraction(cx, prec).to_fraction()
+        cy = MpVal.from_fraction(cy, prec).to_fraction()
+        width = MpVal.from_fraction(width, prec).to_fraction()
+        cre, cim = [], []
+        for ln in range(H):
+            for ix in range(W):
+                x, y = perturb_c(cx, cy, width, W, H, ix, ln)
+                cre.append(hexfloat(x))
+                cim.append(hexfloat(y))
+        got = [O.points_mpfr(cre, cim, depth, q, fractal=3, threads=THREADS)[0]
+               for q in (prec, 2 * prec, 3 * prec)]
+        agree = float(((got[0] == got[1]) & (got[1] == got[2])).mean())
+        out[name] = got[1].reshape(H, W).astype(np.int32)
+        out[name + "__p"] = got[0].reshape(H, W).astype(np.int32)
+        out[name + "__3p"] = got[2].reshape(H, W).astype(np.int32)
+        meta[name] = dict(fractal=3, cx=hexfloat(cx), cy=hexfloat(cy), width=hexfloat(width),
+                          W=W, H=H, depth=depth, prec=prec, oracle_prec=2 * prec,
+                          kind="resolved" if agree >= 0.99 else "chaotic")
+        print(f"{name}: {time.time() - t0:.1f}s distinct counts {len(np.unique(got[1]))} "
+              f"interior {(got[1] == 0).mean():.2f} p = 2p = 3p on {agree:.4f}", flush=True)
+    np.savez_compressed(GOLD / "perturb_variant.npz", **out)
+    (GOLD / "perturb_variant_views.json").write_text(json.dumps(meta, indent=1))
+
+
 def parse_num(s):
     from mdz_gb300.mpval import parse_number
     return parse_number(s)
@@ -631,7 +689,8 @@ def main(argv: list[str]) -> None:
     for w in what:
         {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
          "perturb": make_perturb, "centres": make_centres, "colour": make_colour,
-         "perturb_fold": make_perturb_fold, "perturb_julia": make_perturb_julia}[w]()
+         "perturb_fold": make_perturb_fold, "perturb_julia": make_perturb_julia,
+         "perturb_variant": make_perturb_variant}[w]()
 
 
 if __name__ == "__main__":
