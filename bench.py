@@ -45,7 +45,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 VIEWS = json.loads((ROOT / "tests" / "golden" / "views.json").read_text())
-ALGO_OPS_PER_PIXEL_ITER = 16   # FP32 ops of one perturbation step
+# FP32 ops of one perturbation step: complex 2 Z dz (4 mul + 2 add), dz^2
+# (3 mul + 2 add), two adds of dc, |z|^2 (2) and its compare
+ALGO_OPS_PER_PIXEL_ITER = 16
 PLAIN_BAND_ROWS = 8            # rows of the frame rendered by the plain MP kernel
 
 
