@@ -1,5 +1,5 @@
-"""Generates the committed golden fixtures and seeded views (run here, where
-the reference sources exist; the GPU machine only reads the outputs).
+"""Generates the committed golden fixtures and seeded views (run where the
+reference sources exist; the GPU tests only read the committed outputs).
 
   python tests/golden/make_golden.py fp64      # fp64_*.npz  (reference double build)
   python tests/golden/make_golden.py views     # views.json  (seeded ray bisection)
