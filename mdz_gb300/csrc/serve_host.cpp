@@ -6,17 +6,20 @@
 //     the fixed-point pixel coordinates, footprint; queue it.
 //   admit (engine thread, arrival order): a slot, a piece of the device arena,
 //     a piece of the pinned staging arena and work-queue room; copy the
-//     inputs; perturbation: launch its reference orbit on the slot's
-//     high-priority stream (the orbit runs beside the steps of other
-//     requests); multi-limb: enqueue its pixels.
-//   orbit finished -> enqueue its pixels.
+//     inputs; perturbation: launch its streamed reference orbit on the
+//     slot's high-priority stream and enqueue its pixels at once (they
+//     iterate up to the last finished orbit entry); multi-limb: enqueue its
+//     pixels.
 //   steps: every queued pixel of every request advances by at most its
 //     request's budget of iterations (budgets give each running request an
-//     equal share of the step).
-//   all pixels finished -> perturbation: the FP64 and multi-limb
-//     escalation passes over the flagged pixels on the slot's stream; then
+//     equal share of the step, scaled by the measured slice-kernel times).
+//   all pixels finished -> perturbation with flagged pixels: the FP64 and
+//     multi-limb escalation passes, one request at a time in chunks on the
+//     low-priority esc stream; then, once the orbit launch has ended too,
 //     the results are copied to pinned staging, then to the caller's
-//     buffers; the request's memory is released.
+//     buffers; the request's memory is released.  The long kernels (orbit,
+//     passes) report their end in pinned host words: nothing is queued
+//     behind them on any stream.
 #include <math.h>
 #include <string.h>
 
