@@ -1,28 +1,33 @@
-// Perturbation method for deep zooms (Mandelbrot family).
+// Perturbation method for deep zooms.
 //
 // The reference has no perturbation path: its only deep-zoom method is the
-// per-pixel MPFR loop (src/frac_mandel.c:25-52) at img->precision bits.  This
-// file is the new method named for the 2^-1000 workload:
+// per-pixel MPFR loop (src/frac_mandel.c:25-52 and its siblings) at
+// img->precision bits.  This file is the new method named for the 2^-1000
+// workload, for every MDZ formula and both families:
 //
-// 1. Reference orbit.  One orbit Z_{k+1} = Z_k^2 + C (Z_0 = 0, Z_1 = C) of the
-//    frame centre is iterated exactly in multi-limb fixed point by ONE warp.
-//    Numbers are L signed radix-2^28 digits (value = sum d_i 2^(28 i - F),
-//    F = 28 (L-1) fractional bits), so every 28x28-bit partial product fits an
-//    IMAD.WIDE into a 64-bit column sum with no carry chain; the 2L product
-//    columns of Re and Im are spread over the 32 lanes and carries are
-//    resolved with three warp-shuffle passes.  Each Z_k is rounded to FP64
-//    (mantissa pair + int32 exponent, so tiny values near a nucleus keep full
-//    precision) and to FP32 for the pixel loop.
+// 1. Reference orbit.  Z_{k+1} = f(Z_k) + C (Z_0 = 0, Z_1 = C; Julia:
+//    Z_0 = the view centre, C = the Julia constant) iterated exactly in
+//    multi-limb fixed point by four warps (orbit_produce).  Numbers are L
+//    signed radix-2^28 digits (value = sum d_i 2^(28 i - F), F = 28 (L-1)),
+//    so every 28x28-bit product fits an IMAD.WIDE into a 64-bit column sum;
+//    the columns of Re and Im are spread over the lanes and carries are
+//    resolved with warp-shuffle passes.  The folds (burning ship, celtic, the
+//    variant's odd steps) take their signs from the digits.  A finisher
+//    rounds each Z_k to FP64 (mantissa pair + int32 exponent) and FP32 and
+//    stores the exact |Z_k|^2 - 4 and, for the folded formulas, the fold
+//    quantity and its exact sign.
 //
 // 2. Pixels.  dz = z - Z_m is kept as an FP32 mantissa pair t with an int32
-//    exponent e (dz = t 2^e).  The hot step is plain FP32:
+//    exponent e (dz = t 2^e).  The Mandelbrot hot step is plain FP32:
 //        t' = 2 Z_m t + 2^e t^2 + dc 2^-e
 //    with 2^e and dc 2^-e refreshed only when |t| leaves [2^-32, 2^32].
 //    FP64 is used only where precision is lost otherwise: the rebase test
-//    |Z_m + dz| < |dz| (screened in FP32: it can only hold when
-//    |dz| >= |Z_m| / 2), the rebase itself dz <- Z_m + dz, m <- 0 (Zhuoran's
-//    rebasing), and the full floatexp step needed when Z_m is tiny and dz is
-//    below the FP32 range.  Escape: |Z_m + dz|^2 > 4, evaluated in FP32.
+//    |Z_m + dz| < |dz| (screened in FP32), the rebase itself
+//    dz <- Z_m + dz, m <- 0 (Zhuoran's rebasing), the full floatexp step
+//    when Z_m is tiny and dz is below the FP32 range, escape decisions
+//    within 2^-14 of the bailout, and the folded formulas' steps near their
+//    fold.  Pixels that lose too much precision are re-run with FP64
+//    mantissas, then on the exact multi-limb kernel (perturb_run).
 //
 // Counts follow MDZ's convention (src/frac_mandel.c:11-20): z starts at c,
 // the first update is iteration 1, the count is the first iteration whose
