@@ -1057,6 +1057,28 @@ int Server::enqueue_copies(const std::shared_ptr<Req>& r)
 
 int Server::advance_finishing()
 {
+    // a cancel after the main pass: no further passes, no copies to the
+    // caller (a pass in flight ends first; copies already queued land in
+    // staging only)
+    for (auto& slot_ref : slots) {
+        auto r = slot_ref;
+        if (!r || r->phase <= kRunning || r->cancelled)
+            continue;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (!r->cancel)
+                continue;
+        }
+        r->cancelled = true;
+        if (r->phase == kEscWait) {
+            for (auto it = esc_fifo.begin(); it != esc_fifo.end(); ++it)
+                if (*it == r) {
+                    esc_fifo.erase(it);
+                    break;
+                }
+            r->phase = kCopyWait;
+        }
+    }
     // results of requests whose kernels have all ended
     for (auto& slot_ref : slots) {
         auto r = slot_ref;
@@ -1075,7 +1097,10 @@ int Server::advance_finishing()
         auto r = esc_cur;
         const int v = *hflag(r, r->phase == kEscFp64 ? 20 : 24);
         int rc = MDZGPU_OK;
-        if (v == 1) {
+        if (v != 0 && r->cancelled) {
+            esc_cur = nullptr;   // cancelled: its memory goes once the orbit ended
+            r->phase = kCopyWait;
+        } else if (v == 1) {
             rc = launch_escalation(r, r->phase == kEscMp);
         } else if (v == 3 && r->phase == kEscFp64) {
             r->phase = kEscMp;

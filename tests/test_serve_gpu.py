@@ -242,6 +242,39 @@ def test_serve_cancel_running(server):
     assert run_alone(server, small)["state"] == "done"
 
 
+def test_serve_cancel_after_main_pass(server):
+    """A cancel that arrives while a request's escalation passes run (its
+    steps no longer advance): no further pass, the caller's buffer is never
+    written, the engine carries on."""
+    m = json.loads((Path(__file__).resolve().parent / "golden" /
+                    "perturb_fold_views.json").read_text())["f_ship_a300"]
+    prec, W, H = m["prec"], 1280, 720
+    req = RenderRequest(W, H, m["depth"], MpVal.from_fraction(parse_number(m["cx"]), prec),
+                        MpVal.from_fraction(parse_number(m["cy"]), prec),
+                        MpVal.from_fraction(parse_number(m["width"]) * Fraction(W, m["W"]),
+                                            prec), prec, fractal=1)
+    req.counts = np.full((H, W), -7, np.int32)
+    rid = server.submit(req)
+    t0 = time.time()
+    last, since = -1, time.time()
+    while time.time() - t0 < 60:
+        st = server.poll(rid)
+        if st["state"] != "running" and st["state"] != "queued":
+            break
+        if st["steps"] != last:
+            last, since = st["steps"], time.time()
+        elif last > 0 and time.time() - since > 0.05:
+            break   # steps stopped: the main pass is over
+        time.sleep(0.002)
+    server.cancel(rid)
+    st = server.wait(rid, 60_000)
+    assert st["state"] in ("cancelled", "done"), st
+    if st["state"] == "cancelled":
+        assert (req.counts == -7).all()
+    small = view_request("p_gal_polyp")
+    assert run_alone(server, small)["state"] == "done"
+
+
 def test_serve_timeout(server):
     req = heavy_request(timeout_ms=300.0)
     rid = server.submit(req)
