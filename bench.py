@@ -48,7 +48,10 @@ VIEWS = json.loads((ROOT / "tests" / "golden" / "views.json").read_text())
 # FP32 ops of one perturbation step: complex 2 Z dz (4 mul + 2 add), dz^2
 # (3 mul + 2 add), two adds of dc, |z|^2 (2) and its compare
 ALGO_OPS_PER_PIXEL_ITER = 16
-PLAIN_BAND_ROWS = 8            # rows of the frame rendered by the plain MP kernel
+# rows of the frame rendered by the plain multi-limb kernel: 1920 x 64 pixels
+# = 3840 warps of 8x4-pixel tiles, about three full waves of the resident
+# warps at 34 words (240 registers: 8 warps per SM x 152 SMs)
+PLAIN_BAND_ROWS = 64
 
 
 def parse_args():
@@ -138,6 +141,16 @@ def c4_values(view):
     return cx, cy, width, prec
 
 
+def workload_config(view, world: int) -> dict:
+    """The `config` object both arms print (identical, so the two lines
+    describe the same workload)."""
+    return {"workload": f"c4: {view['width']}x{view['height']}, width 2^-1000, "
+                        f"{view['precision']}-bit centre (seeded ray bisection), "
+                        f"maxiter {view['depth']}, Mandelbrot",
+            "l2": "flushed between steps (256 MB write)",
+            "parallelism": f"replicas x{world}"}
+
+
 def dist_init(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -212,10 +225,11 @@ def run_reference(args, view, world, rank, dist):
     line = {"metric": "pixel-iters/s at 2^-1000 zoom", "impl": "reference", "value": value,
             "unit": "pixel-iters/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "mpfr-1088", "data": "synthetic",
-            "config": {"workload": "c4: 1920x1080, width 2^-1000, 1088-bit centre, "
-                                   "maxiter 200000, Mandelbrot",
-                       "path": "reference per-pixel MPFR loop (frac_mandel_mpfr) on host cores"},
+            "vs_baseline": None, "dtype": f"mpfr-{view['precision']}", "data": "synthetic",
+            "config": workload_config(view, world),
+            "path": "the reference's per-pixel MPFR loop (frac_mandel_mpfr) restated in "
+                    "oracle/mdz_oracle.c, on host cores; each step a bounded random-pixel "
+                    "sample of the frame",
             "cpu_baseline": dict(base, value=value),
             "e2e": {"value": value, "unit": "pixel-iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -432,11 +446,9 @@ def run_ours(args, view, world, rank, local, dist):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32+int32 floatexp (fp64 rebase)", "data": "synthetic",
-        "config": {"workload": "c4: 1920x1080, width 2^-1000, 1088-bit centre (seeded ray "
-                               "bisection), maxiter 200000, Mandelbrot, perturbation",
-                   "orbit_limbs": int(lib.mdzgpu_perturb_limbs(prec)), "orbit_len": orbit_len,
-                   "l2": "flushed between steps (256 MB write)",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(view, world),
+        "method": {"name": "perturbation", "orbit_limbs": int(lib.mdzgpu_perturb_limbs(prec)),
+                   "orbit_len": orbit_len},
         "gpu_launches": launches * args.steps,
         "orbit_ms": (sum(orbit_ms) / len(orbit_ms)) if min(orbit_ms) >= 0 else "fused",
         "rebases_per_step": rebases / args.steps,

@@ -177,14 +177,18 @@ int mdzgpu_render_mp_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f,
  * host application's pool allocator owns the device, or a render loop that
  * cannot take cudaMalloc's implicit device synchronisation).  Same inputs and
  * results as mdzgpu_render_mp_device; d_counts is the caller's device buffer
- * of width*height int32; the work is queued on `stream` (a cudaStream_t,
- * NULL = default stream) and not waited for.  Scratch is a fixed 1.13 MiB
- * array per GPU inside the library, held until the process exits: frames
- * with width + height > 8192 or needing more than 36 words are rejected
- * (MDZGPU_ERR_ARG).  Calls on one stream are ordered; calls that may overlap
- * on the GPU (other streams or threads) race on the shared scratch and must
- * not be made.  The first call on each device looks up the scratch address
- * (with that device current); make it before capturing a stream. */
+ * of width*height int32; the kernel is queued on `stream` (a cudaStream_t,
+ * NULL = default stream).  The coordinate tables are copied from a temporary
+ * (pageable) host buffer, so the call may block until the work queued
+ * earlier on that stream has finished.  Scratch is a fixed 1.13 MiB array
+ * per GPU inside the library, held until the process exits: frames with
+ * width + height > 8192 or needing more than 36 words are rejected
+ * (MDZGPU_ERR_ARG); a Julia constant outside |x|, |y| < 4 is rejected with
+ * MDZGPU_ERR_RANGE, as by mdzgpu_render_mp_device.  Calls on one stream are
+ * ordered; calls that may overlap on the GPU (other streams or threads) race
+ * on the shared scratch and must not be made.  The first call in each CUDA
+ * context (the current one: the device's primary context or the caller's
+ * own) looks up the scratch address; make it before capturing a stream. */
 int mdzgpu_render_mp_noalloc(const mdzgpu_frame* f, const mdzgpu_mpval* xmin,
                              const mdzgpu_mpval* ymax,
                              const mdzgpu_mpval* width,
@@ -213,6 +217,15 @@ int mdzgpu_colour(mdzgpu_ctx* ctx, const int32_t* counts, int32_t real_w,
 int mdzgpu_colour_device(mdzgpu_ctx* ctx, const int32_t* d_counts,
                          int32_t real_w, int32_t real_h, int32_t aa,
                          const mdzgpu_palette* pal, uint32_t* d_rgb);
+
+/* No counterpart in the reference.  Polls a bounded device wait of this
+ * context's perturbation launches makes before it gives up (the orbit
+ * finisher waiting for the producer, the fused launch's pixels waiting for
+ * finished orbit entries); 0 restores the default (2^25 polls of >= 256 ns,
+ * several seconds).  A wait that gives up sets the launch's error word, the
+ * kernel returns, and the call reports MDZGPU_ERR_TIMEOUT.  Small values
+ * exist to test that path. */
+int mdzgpu_set_wait_limit(mdzgpu_ctx* ctx, int32_t polls);
 
 /* Largest `words` value the MP kernel is built for. */
 int32_t mdzgpu_mp_max_words(void);

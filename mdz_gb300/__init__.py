@@ -15,7 +15,7 @@ import numpy as np
 from . import native
 from .mpval import MpVal, hexfloat, parse_number
 from .native import Frame, NativeUnavailable, Stats
-from .views import Rect, View, mdz_rect
+from .views import Rect, View, mdz_rect, perturb_half_spacing
 
 __all__ = ["Renderer", "MpVal", "View", "Rect", "mdz_rect", "NativeUnavailable", "hexfloat",
            "parse_number", "MDZ_FAMILY", "MDZ_FRACTAL"]
@@ -166,9 +166,10 @@ class Renderer:
         return st.as_dict()
 
 
-def perturb_spacing(width: MpVal, W: int) -> tuple[int, int]:
-    """(hs_m, hs_e) of the perturbation path's half pixel spacing, as the
-    library computes it: width / (2 W) rounded to 40 significant bits."""
+def perturb_spacing(width: MpVal, W: int) -> tuple[float, int]:
+    """(hs_m, hs_e) of the perturbation path's half pixel spacing as the
+    library computes it (mdzgpu_perturb_spacing): width / (2 W) rounded to 40
+    significant bits."""
     lib = native.load()
     s, keep = width.struct()
     m = C.c_double()
@@ -179,8 +180,9 @@ def perturb_spacing(width: MpVal, W: int) -> tuple[int, int]:
 
 
 def perturb_pixel_c(cx: MpVal, cy: MpVal, width: MpVal, W: int, H: int, ix: int, line: int):
-    """Exact c of pixel (ix, line) in the perturbation path's geometry."""
+    """Exact c of pixel (ix, line) in the perturbation path's geometry
+    (computed in Python: the library is not loaded)."""
     from fractions import Fraction
-    hs_m, hs_e = perturb_spacing(width, W)
+    hs_m, hs_e = perturb_half_spacing(width, W)
     hs = Fraction(hs_m) * Fraction(2) ** hs_e
     return (cx.to_fraction() + (2 * ix - W) * hs, cy.to_fraction() + (H - 2 * line) * hs)

@@ -535,6 +535,16 @@ int mdzgpu_perturb_spacing(const mdzgpu_mpval* width, int32_t W, double* hs_m, i
     return rc;
 }
 
+int mdzgpu_set_wait_limit(mdzgpu_ctx* ctx, int32_t polls)
+{
+    if (!ctx || polls < 0) {
+        set_error("wait limit: null context or negative poll count");
+        return MDZGPU_ERR_ARG;
+    }
+    ctx->wait_limit = polls ? polls : kSpinLimit;
+    return MDZGPU_OK;
+}
+
 int32_t mdzgpu_perturb_limbs(int64_t precision)
 {
     long L = (long)((precision + 27) / 28) + 1;
@@ -787,6 +797,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.fm = (double*)(ob + ol.fm);
     o.fe = (int*)(ob + ol.fe);
     o.axis = (unsigned*)(ob + ol.axis);
+    o.spin_limit = ctx->wait_limit;
     OrbitLaunch oq = o;   // Julia: the critical orbit; hybrid: the even-step one
     if (two) {
         if (julia) {
@@ -883,6 +894,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.sync = (FrameSync*)ctx->sync.ptr;
     p.rebases = (unsigned long long*)(ob + off_reb);
     p.stop = nullptr;
+    p.spin_limit = ctx->wait_limit;
     // escalation lists: [count1 | count2 | pad] list1[n] list2[n]
     if ((rc = ctx->lists.ensure(256 + 2 * n * sizeof(unsigned)))) {
         cudaEventDestroy(evo);

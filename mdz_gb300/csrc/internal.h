@@ -99,9 +99,16 @@ struct mdzgpu_ctx {
     mdz::DevBuf pqueue;     // step counters + two pixel queues
     mdz::PinnedBuf stepinfo;  // step results read by the host
     mdz::DevBuf palette;    // colouring: up to 256 colours
+    // polls a bounded device wait makes before it gives up (mdz::kSpinLimit
+    // unless mdzgpu_set_wait_limit changed it)
+    int wait_limit = 1 << 25;
 };
 
 namespace mdz {
+
+// Bounded device waits: ~2^25 polls of >= 256 ns (several seconds), far
+// beyond any legitimate wait, then the launch's error flag is raised.
+constexpr int kSpinLimit = 1 << 25;
 
 struct Fp64Launch {
     int W, H;           // real frame size
@@ -139,6 +146,8 @@ struct MpLaunch {
                             // (3 when it also reached the list's end)
     // list pass in chunks: this launch takes tiles tile_base + [0, tile_limit)
     unsigned tile_base = 0, tile_limit = 0xffffffffu;
+    // polls a bounded wait of the fused launch makes before it gives up
+    int spin_limit = kSpinLimit;
 };
 int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
 bool mp_words_supported(int words);
@@ -187,6 +196,9 @@ struct OrbitLaunch {
     // MDZ_VARIANT (celtic fold on odd iterations, src/frac_variant.c:14-17):
     // the step Z_k -> Z_{k+1} folds when k % 2 == fold_parity
     int fold_parity = 1;
+    // polls the finisher's bounded wait for the producer makes before it
+    // gives up (sets progress[4])
+    int spin_limit = kSpinLimit;
 };
 int launch_orbit(const OrbitLaunch& p, cudaStream_t s);
 int orbit_max_limbs();
@@ -239,6 +251,8 @@ struct PerturbLaunch {
                                  // (3 when it also reached the list's end)
     // list pass in chunks: this launch takes tiles tile_base + [0, tile_limit)
     unsigned tile_base = 0, tile_limit = 0xffffffffu;
+    // polls a bounded wait of the fused launch makes before it gives up
+    int spin_limit = kSpinLimit;
 };
 // pass 0: FP32 frame pass; pass 1: FP64 pass over list_in
 int launch_perturb(mdzgpu_ctx* ctx, const PerturbLaunch& p, cudaStream_t s, int pass);

@@ -21,9 +21,18 @@
 // GPU (different streams, or different host threads) race on the array and
 // must not be made.
 //
-// First call per device: looks up the array's device address with
-// cudaGetSymbolAddress while that device is current (and caches it).  Make
-// that first call before capturing any stream into a CUDA graph.
+// Host blocking: the coordinate tables are built in a temporary host buffer
+// and copied from there (pageable memory), so the call may wait until the
+// work queued earlier on the stream has finished before it returns.
+//
+// Set-up: the array's device address is looked up with cudaGetSymbolAddress
+// once per CUDA context (keyed by the context's process-unique id, so a
+// caller's own non-primary context, or the new primary context after
+// cudaDeviceReset, gets its own lookup) while that context is current.  The
+// first call in a context does this; make it before capturing any stream
+// into a CUDA graph.
+#include <cuda.h>
+
 #include <mutex>
 #include <vector>
 
@@ -41,29 +50,92 @@ constexpr size_t kScratchWords = kSyncBytes / 4 + kTableWords;
 // [FrameSync | xs[W][words] | ys[H][words] | julia[2][words]]
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kScratchWords];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-// Device address of g_noalloc_scratch on the current device (set-up once per
-// device; the device must be current).
-int scratch_address(int device, uint32_t** out)
+constexpr int kMaxContexts = 64;
+std::mutex g_setup_mutex;
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    void* ptr;
+};
+ScratchEntry g_scratch_addr[kMaxContexts] = {};
+int g_scratch_entries = 0;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+int driver_entry_points()
+{
+    if (g_ctx_get_current && g_ctx_get_id)
+        return MDZGPU_OK;
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa = cudaDriverEntryPointSymbolNotFound, qb = qa;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa)
+            != cudaSuccess
+        || cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb)
+            != cudaSuccess
+        || qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b) {
+        set_error("no-alloc render: the driver does not provide cuCtxGetCurrent / cuCtxGetId");
+        return MDZGPU_ERR_CUDA;
+    }
+    g_ctx_get_current = (CtxGetCurrentFn)a;
+    g_ctx_get_id = (CtxGetIdFn)b;
+    return MDZGPU_OK;
+}
+
+// Device address of g_noalloc_scratch in the current context (looked up once
+// per context, with that context current).
+int scratch_address(uint32_t** out)
 {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (device < 0 || device >= kMaxDevices) {
-        set_error("no-alloc render: device %d out of range", device);
-        return MDZGPU_ERR_ARG;
+    int rc = driver_entry_points();
+    if (rc)
+        return rc;
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) {
+        set_error("no-alloc render: cuCtxGetCurrent failed");
+        return MDZGPU_ERR_CUDA;
     }
-    if (!g_scratch_addr[device]) {
-        void* ptr = nullptr;
+    void* ptr = nullptr;
+    if (!ctx) {
+        // no context yet on this thread: the runtime makes the device's
+        // primary context current while it resolves the symbol
         const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess || !ptr) {
             set_error("no-alloc render: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return MDZGPU_ERR_CUDA;
         }
-        g_scratch_addr[device] = ptr;
+        if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) {
+            set_error("no-alloc render: no current CUDA context");
+            return MDZGPU_ERR_CUDA;
+        }
     }
-    *out = (uint32_t*)g_scratch_addr[device];
+    unsigned long long id = 0;
+    if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) {
+        set_error("no-alloc render: cuCtxGetId failed");
+        return MDZGPU_ERR_CUDA;
+    }
+    for (int i = 0; i < g_scratch_entries; ++i)
+        if (g_scratch_addr[i].ctx_id == id) {
+            *out = (uint32_t*)g_scratch_addr[i].ptr;
+            return MDZGPU_OK;
+        }
+    if (!ptr) {
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            set_error("no-alloc render: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return MDZGPU_ERR_CUDA;
+        }
+    }
+    // remember it; when the table is full the oldest entry makes room
+    if (g_scratch_entries == kMaxContexts) {
+        for (int i = 1; i < kMaxContexts; ++i)
+            g_scratch_addr[i - 1] = g_scratch_addr[i];
+        --g_scratch_entries;
+    }
+    g_scratch_addr[g_scratch_entries++] = {id, ptr};
+    *out = (uint32_t*)ptr;
     return MDZGPU_OK;
 }
 
@@ -99,7 +171,7 @@ extern "C" int mdzgpu_render_mp_noalloc(const mdzgpu_frame* f, const mdzgpu_mpva
     int device = 0;
     MDZ_CUDA_TRY(cudaGetDevice(&device));
     uint32_t* scratch = nullptr;
-    int rc = scratch_address(device, &scratch);
+    int rc = scratch_address(&scratch);
     if (rc)
         return rc;
     int sms = 0;
@@ -115,7 +187,9 @@ extern "C" int mdzgpu_render_mp_noalloc(const mdzgpu_frame* f, const mdzgpu_mpva
         rc = mpfr_round_to_fixed(julia_re, (long)precision, w, tab.data() + (size_t)(W + H) * w)
              | mpfr_round_to_fixed(julia_im, (long)precision, w,
                                    tab.data() + (size_t)(W + H + 1) * w);
-    if (rc) {
+    if (rc || (f->family == MDZ_FAMILY_JULIA
+               && (!fx_fits_coordinate(tab.data() + (size_t)(W + H) * w, w)
+                   || !fx_fits_coordinate(tab.data() + (size_t)(W + H + 1) * w, w)))) {
         set_error("no-alloc render: coordinates must satisfy |x|, |y| < 4");
         return MDZGPU_ERR_RANGE;
     }

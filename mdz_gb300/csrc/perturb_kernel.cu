@@ -44,9 +44,6 @@ constexpr int kTileW = 8;
 constexpr int kTileH = 4;
 constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
 constexpr int kOrbitThreads = 128;  // producer threads (four warps)
-// Bounded waits of the fused launch: ~2^25 polls of >= 256 ns (several
-// seconds), far beyond any legitimate wait, then the error flag is raised.
-constexpr int kSpinLimit = 1 << 25;
 
 // --------------------------------------------------------------------------
 // Reference orbit
@@ -501,7 +498,7 @@ __device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
                 r = d ? *(volatile int*)p.out_len : *(volatile int*)g.raw_len;
                 if (d || r >= fin + 256)
                     break;
-                if (*(volatile int*)g.error || ++spins > kSpinLimit) {
+                if (*(volatile int*)g.error || ++spins > p.spin_limit) {
                     err = 1;
                     break;
                 }
@@ -978,7 +975,7 @@ __device__ __forceinline__ bool wait_orbit(const PerturbLaunch& p, BlockOrbitVie
             __threadfence_block();
             atomicExch(&v->busy, 0);
         }
-        if (*(volatile const int*)p.orbit_error || ++spins > kSpinLimit) {
+        if (*(volatile const int*)p.orbit_error || ++spins > p.spin_limit) {
             atomicExch(p.orbit_error, 1);
             return false;
         }
@@ -1639,7 +1636,7 @@ __global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, Pe
     __shared__ int s_leave;
     if (threadIdx.x == 0) {
         int sm = 0, spins = 0;
-        while ((sm = *(volatile const int*)p.producer_sm) == 0 && ++spins < kSpinLimit)
+        while ((sm = *(volatile const int*)p.producer_sm) == 0 && ++spins < p.spin_limit)
             __nanosleep(64);
         s_leave = (sm == (int)smid + 1);
     }

@@ -129,3 +129,23 @@ class View:
         extra = dict(d.get("extra") or {})
         extra.update({k: v for k, v in d.items() if k not in keys and k != "extra"})
         return View(**{k: v for k, v in d.items() if k in keys}, extra=extra)
+
+
+def perturb_half_spacing(width: MpVal, W: int) -> tuple[float, int]:
+    """Half pixel spacing of the perturbation geometry, (hs_m, hs_e) with
+    hs = hs_m * 2^hs_e: the top 53 bits of `width` (truncated), divided by
+    2 W in double (round to nearest), then rounded to 40 significant bits
+    (ties to even), so that (2 ix - W) * hs is exact in FP64 for every pixel.
+    Pure Python; the library's mdzgpu_perturb_spacing computes the same."""
+    import math
+    if width.mant <= 0 or W <= 0:
+        raise ValueError("perturbation needs a positive width")
+    n = width.nlimbs
+    top = width.mant >> (64 * (n - 1))
+    mant = float(top >> 11)                   # exact: 53 bits
+    e0 = width.exp - 53
+    q = mant / (2.0 * W)
+    k = math.frexp(q)[1] - 1                  # ilogb
+    m = math.ldexp(q, -k)                     # [1, 2)
+    m = math.ldexp(float(round(math.ldexp(m, 39))), -39)
+    return m, e0 + k

@@ -17,7 +17,16 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 LIB = OUT / "libmdzoracle.so"
-REF_SRC = Path(os.environ.get("MDZ_REF_SRC", "/root/reference/src"))
+
+
+def ref_root() -> Path | None:
+    """The MDZ source tree the reference build and the fixture scripts read
+    (MDZ_REF_ROOT, else the default oracle/build_ref.sh names), or None when
+    it is not on this machine."""
+    r = subprocess.run(["sh", str(HERE / "build_ref.sh"), "--root"], capture_output=True,
+                       text=True)
+    root = Path(r.stdout.strip()) if r.returncode == 0 and r.stdout.strip() else None
+    return root if root is not None and (root / "src" / "fractal.c").exists() else None
 
 
 def find_system_lib(name: str) -> str | None:
@@ -48,7 +57,7 @@ def build(reference: bool = True) -> Path:
         cmd += ["-lm", "-lpthread"]
         subprocess.run(cmd, check=True)
         stamp.write_text(variant)
-    if reference and (REF_SRC / "fractal.c").exists() and platform.machine() == "x86_64":
+    if reference and ref_root() is not None and platform.machine() == "x86_64":
         subprocess.run(["sh", str(HERE / "build_ref.sh")], check=True,
                        stdout=subprocess.DEVNULL)
     return LIB

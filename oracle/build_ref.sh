@@ -1,8 +1,8 @@
 #!/bin/sh
 # Build the UNMODIFIED MDZ hot path into oracle/_ref/ (TEST INFRASTRUCTURE).
 #
-# Compiles the reference's own sources where they lie (default
-# /root/reference/src, override with MDZ_REF_SRC) with the declaration-only
+# Compiles the reference's own sources where they lie (the MDZ tree at
+# MDZ_REF_ROOT, default /root/reference; sources in its src/) with the declaration-only
 # headers in oracle/shim/ and links them against the system libmpfr.so.6 /
 # libgmp.so.10 by full path (no -dev packages are needed).  Two variants:
 #   libmdzref_d.so   long double mapped to IEEE double, no FMA contraction
@@ -12,9 +12,13 @@
 #   libmdzref_ld.so  as shipped (x87 80-bit long double on x86-64).
 # Only x86-64 has -mlong-double-64; elsewhere the script exits 0 without
 # building (the oracle restatement in oracle/mdz_oracle.c covers that case).
+# `build_ref.sh --root` prints the tree's location and exits (the Python
+# side asks here, so this recipe is the one place that names it).
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-SRC=${MDZ_REF_SRC:-/root/reference/src}
+REF_ROOT=${MDZ_REF_ROOT:-/root/reference}
+if [ "$1" = "--root" ]; then echo "$REF_ROOT"; exit 0; fi
+SRC="$REF_ROOT/src"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC/fractal.c" ]; then
     echo "build_ref: no reference sources at $SRC; skipping" >&2

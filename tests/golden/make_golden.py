@@ -11,6 +11,7 @@ reference sources exist; the GPU tests only read the committed outputs).
   python tests/golden/make_golden.py perturb_fold  # perturb_fold.npz (ship / celtic, MPFR 2p)
   python tests/golden/make_golden.py perturb_julia # perturb_julia.npz (Julia family, MPFR 2p)
   python tests/golden/make_golden.py perturb_variant  # perturb_variant.npz (hybrid, MPFR 2p)
+  python tests/golden/make_golden.py c2        # c2_frame.json + c2_rows.npz (full config-2 frame)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -93,6 +94,31 @@ def make_fp64() -> None:
             for v in fp64_views()}
     np.savez_compressed(GOLD / "fp64_counts.npz", **out)
     (GOLD / "fp64_views.json").write_text(json.dumps(meta, indent=1, default=str))
+
+
+C2_ROW_STEP = 27
+
+
+def make_c2() -> None:
+    """The seeded 1920x1080 view with 3x3 supersampling (5760x3240 counts),
+    width 1e-11, maxiter 20000, rendered in full by the unmodified reference
+    (double build without FMA, rth_* thread pool): the frame's sha256 and
+    iteration total, and every 27th row (rows 0, 27, ..., 3213) as the
+    committed comparison data."""
+    views = json.loads((GOLD / "views.json").read_text())
+    v = View.from_dict({k: x for k, x in views["c2"].items() if k != "seed"})
+    t0 = time.time()
+    ref, t_ref = O.ref_render(v, threads=THREADS, variant="d")
+    rows = ref[::C2_ROW_STEP]
+    meta = {"view": views["c2"], "shape": list(ref.shape), "sha256": sha(ref),
+            "pixel_iters": pixel_iters(ref, v.depth), "row_step": C2_ROW_STEP,
+            "rows": len(rows), "rect": [hexfloat(Fraction(x)) for x in v.rect().doubles()],
+            "source": "oracle/_ref/libmdzref_d.so (unmodified MDZ, long double = double, "
+                      f"no FMA), rth_* with {THREADS} threads",
+            "reference_render_s": round(t_ref, 1)}
+    np.savez_compressed(GOLD / "c2_rows.npz", rows=rows)
+    (GOLD / "c2_frame.json").write_text(json.dumps(meta, indent=1))
+    print(f"c2: {ref.shape} iters={meta['pixel_iters']} ({time.time() - t0:.1f}s)")
 
 
 # --------------------------------------------------------------------------
@@ -220,7 +246,7 @@ def make_colour() -> None:
     from mdz_gb300.mdzfile import load as load_mdz
     rng = np.random.Generator(np.random.PCG64(2024))
     cases = []
-    for f in sorted(GALLERY.glob("*.mdz")):
+    for f in sorted(_gallery().glob("*.mdz")):
         try:
             s = load_mdz(f)
         except Exception:
@@ -281,7 +307,13 @@ def mdz_mpfr_c(v: View, prec: int, ix: int, line: int) -> tuple[Fraction, Fracti
     return x, y
 
 
-GALLERY = Path("/root/reference/gallery")
+def _gallery() -> Path:
+    from oracle.build import ref_root
+    root = ref_root()
+    if root is None:
+        raise SystemExit("make_golden: the MDZ source tree is not on this machine "
+                         "(set MDZ_REF_ROOT)")
+    return root / "gallery"
 
 
 def gallery_views(width: int = 64) -> list[View]:
@@ -289,7 +321,7 @@ def gallery_views(width: int = 64) -> list[View]:
     pixels across; rect-form files are turned into centre/size exactly."""
     from mdz_gb300.mpval import parse_number
     vs = []
-    for f in sorted(GALLERY.glob("*.mdz")):
+    for f in sorted(_gallery().glob("*.mdz")):
         kv = {}
         for line in f.read_text().splitlines():
             parts = line.split(None, 1)
@@ -690,7 +722,7 @@ def main(argv: list[str]) -> None:
         {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
          "perturb": make_perturb, "centres": make_centres, "colour": make_colour,
          "perturb_fold": make_perturb_fold, "perturb_julia": make_perturb_julia,
-         "perturb_variant": make_perturb_variant}[w]()
+         "perturb_variant": make_perturb_variant, "c2": make_c2}[w]()
 
 
 if __name__ == "__main__":

@@ -12,10 +12,12 @@ import pytest
 
 from mdz_gb300 import MpVal, native
 from mdz_gb300 import abi
+from oracle.build import ref_root
 
 ROOT = Path(__file__).resolve().parents[1]
 GOLD = ROOT / "tests" / "golden"
-REF_SRC = Path("/root/reference/src")
+_REF_ROOT = ref_root()
+REF_SRC = _REF_ROOT / "src" if _REF_ROOT else ROOT / "oracle" / "_absent"
 
 
 def declared_functions():
@@ -181,3 +183,22 @@ def test_mp_coordinates_equal_mpfr_roundings(prec, cx, cy, size, W, H):
     for ln in range(H):
         _, y = mpfr_pixel_c(r, W, prec, 0, ln)
         assert fixed(ys, ln) == y
+
+
+def test_python_half_spacing_equals_library():
+    """The perturbation geometry's 40-bit half spacing, computed in Python
+    (used where the library must not be loaded: the CPU baseline), equals
+    mdzgpu_perturb_spacing on seeded widths and frame sizes."""
+    from mdz_gb300 import perturb_spacing
+    from mdz_gb300.views import perturb_half_spacing
+    rng = np.random.default_rng(17)
+    cases = [(MpVal.from_fraction(Fraction(2) ** -1000, 1088), 1920),
+             (MpVal.from_fraction(Fraction(3), 80), 240)]
+    for _ in range(300):
+        e = int(rng.integers(-1100, 3))
+        num = int(rng.integers(1, 1 << 62))
+        prec = int(rng.choice([64, 80, 256, 1088, 2176]))
+        W = int(rng.integers(1, 8000))
+        cases.append((MpVal.from_fraction(Fraction(num, 1 << 62) * Fraction(2) ** e, prec), W))
+    for w, W in cases:
+        assert perturb_half_spacing(w, W) == perturb_spacing(w, W), (w, W)

@@ -11,11 +11,13 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from oracle.build import ref_root
 
 ROOT = Path(__file__).resolve().parents[1]
 GOLD = ROOT / "tests" / "golden"
 REF_IO = ROOT / "oracle" / "_ref" / "libmdzref_io.so"
-GALLERY = Path("/root/reference/gallery")
+_REF_ROOT = ref_root()
+GALLERY = _REF_ROOT / "gallery" if _REF_ROOT else ROOT / "oracle" / "_absent"
 META = json.loads((GOLD / "colour.json").read_text())
 DATA = np.load(GOLD / "colour.npz")
 

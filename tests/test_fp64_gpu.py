@@ -1,5 +1,6 @@
 """FP64 path on the GPU: bit-exact against the reference's double build
 (counts from the unmodified MDZ rth_* + fractal.c, tests/golden)."""
+import hashlib
 import json
 from fractions import Fraction
 from pathlib import Path
@@ -85,3 +86,45 @@ def test_fp64_device_output(renderer):
     torch.cuda.synchronize()
     assert np.array_equal(buf.cpu().numpy(), COUNTS["deep"])
     assert st["d2h_bytes"] <= 64
+
+
+def _c2():
+    path = GOLD / "c2_frame.json"
+    if not path.exists():
+        pytest.skip("c2 fixture not generated")
+    meta = json.loads(path.read_text())
+    v = View.from_dict({k: x for k, x in meta["view"].items() if k != "seed"})
+    return v, meta, np.load(GOLD / "c2_rows.npz")["rows"]
+
+
+def test_c2_full_frame_explicit_bit_exact(renderer):
+    """The seeded 1920x1080, 3x3-supersampled frame (5760x3240 counts, width
+    1e-11, maxiter 20000) in full against the unmodified reference's double
+    build without FMA (src/fractal.c:29-117, src/frac_mandel.c:5-21): the
+    frame's sha256, its iteration total and every 27th row."""
+    v, meta, rows = _c2()
+    xmin, xmax, ymax = (float(parse_number(s)) for s in meta["rect"])
+    got, st = renderer.render_fp64(v.real_width, v.real_height, v.depth, xmin, xmax, ymax)
+    assert list(got.shape) == meta["shape"]
+    step = meta["row_step"]
+    bad = [i * step for i in range(len(rows)) if not np.array_equal(got[i * step], rows[i])]
+    assert not bad, f"rows differ: {bad[:10]}"
+    assert st["pixel_iters"] == meta["pixel_iters"]
+    assert hashlib.sha256(got.tobytes()).hexdigest() == meta["sha256"]
+
+
+def test_c2_full_frame_dropin_bit_exact():
+    """The same frame through MDZ's own entry points (rth_ui_start_render
+    with fractal_calculate_line installed, as image_info_set_multi_prec
+    does for the hardware-float path)."""
+    v, meta, rows = _c2()
+    d = DropIn(v)
+    try:
+        info = d.render(timeout_s=600)
+        assert sorted(info["drawn"]) == list(range(v.height))
+        step = meta["row_step"]
+        bad = [i * step for i in range(len(rows)) if not np.array_equal(d.raw[i * step], rows[i])]
+        assert not bad, f"rows differ: {bad[:10]}"
+        assert hashlib.sha256(d.raw.tobytes()).hexdigest() == meta["sha256"]
+    finally:
+        d.close()

@@ -16,7 +16,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from mdz_gb300 import Renderer, View, native
+from mdz_gb300 import MdzGpuError, Renderer, View, native
 
 pytestmark = pytest.mark.gpu
 
@@ -67,3 +67,29 @@ def test_noalloc_rejects_frames_beyond_its_scratch():
                                       C.c_void_p(out.data_ptr()), None)
     assert rc == -1  # MDZGPU_ERR_ARG, before any device work
     assert "scratch limit" in native.last_error()
+
+
+def test_noalloc_rejects_julia_constant_out_of_range_like_regular_entry_point():
+    """A Julia constant outside the fixed-point coordinate range (|x| < 4) is
+    refused by both entry points with MDZGPU_ERR_RANGE, before any device
+    work; the output buffer keeps its contents."""
+    torch = pytest.importorskip("torch")
+    from mdz_gb300 import MpVal
+    lib = native.load()
+    v = view_of("mp_julia")
+    r = v.rect()
+    W, H = 16, 8
+    big = MpVal.from_fraction(5, 128)
+    jim = MpVal.from_fraction(0, 128)
+    frame = native.Frame(W, H, 1, 0, 100)
+    vals = [x.struct() for x in (r.xmin, r.ymax, r.width, big, jim)]
+    out = torch.full((H, W), -7, dtype=torch.int32, device="cuda")
+    rc = lib.mdzgpu_render_mp_noalloc(C.byref(frame), *[C.byref(s) for s, _ in vals], 128, 0,
+                                      C.c_void_p(out.data_ptr()), None)
+    assert rc == -4, native.last_error()  # MDZGPU_ERR_RANGE
+    with Renderer(0) as rend:
+        with pytest.raises(MdzGpuError, match="error -4"):
+            rend.render_mp_device(W, H, 100, r.xmin, r.ymax, r.width, 128, out.data_ptr(),
+                                  family=1, fractal=0, julia=(big, jim))
+    torch.cuda.synchronize()
+    assert int((out != -7).sum()) == 0
