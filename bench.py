@@ -64,9 +64,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=32,
+    ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests of the seeded mixed stream for the serving latency run "
                          "(0 = skip)")
+    ap.add_argument("--serve-capacity-requests", type=int, default=32,
+                    help="first requests of the stream run closed loop to measure capacity")
     ap.add_argument("--serve-seed", type=int, default=5005)
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the config 2 (FP64) and config 3 (multi-limb) frames")
@@ -301,21 +303,36 @@ def run_plain_configs(args, local) -> dict:
     return out
 
 
+def latency_summary(lat: np.ndarray) -> dict:
+    def pct(q):
+        return float(np.percentile(lat, q, method="inverted_cdf"))
+    return {"n": int(lat.size), "p50": pct(50), "p90": pct(90), "p99": pct(99),
+            "max": float(lat.max()), "mean": float(lat.mean())}
+
+
 def run_serving(args, local) -> dict:
-    """The mixed request stream through the serving engine: first closed
-    loop (all requests submitted at once) to measure the capacity, then
-    Poisson arrivals at `serve_load` of that capacity for p50/p99 latency.
-    The second run's results must equal the first's (each request the same
-    alone or in any mix)."""
+    """The mixed request stream through the serving engine: the first
+    `serve_capacity_requests` requests closed loop (all submitted at once)
+    measure the capacity; then `serve_requests` requests arrive as a Poisson
+    process at `serve_load` of that capacity, for p50/p90/p99 latency (also
+    per image size and per method).  Every request of the closed-loop run
+    must equal its result in the Poisson run (each request the same alone or
+    in any mix).  The engine's own log gives the device time of the steps
+    against their host wall time (the share the step loop and its graph
+    launches add)."""
+    import tempfile
     from mdz_gb300.serve import Server
     from mdz_gb300.stream import load_pool, make_stream
     pool = load_pool()
-    items = make_stream(args.serve_requests, pool, seed=args.serve_seed)
+    items = make_stream(max(args.serve_requests, args.serve_capacity_requests), pool,
+                        seed=args.serve_seed)
 
-    def run(arrivals):
-        reqs = [it.request(pool) for it in items]
+    def run(sel, arrivals):
+        reqs = [items[i].request(pool) for i in sel]
+        with tempfile.NamedTemporaryFile(suffix=".json", delete=False) as tf:
+            log_path = tf.name
         with Server(local, arena_bytes=48 << 30, staging_bytes=2 << 30,
-                    queue_pixels=1 << 25) as srv:
+                    queue_pixels=1 << 25, log_path=log_path) as srv:
             t0 = time.perf_counter()
             ids = []
             for a, rq in zip(arrivals, reqs):
@@ -323,37 +340,49 @@ def run_serving(args, local) -> dict:
                 if dt > 0:
                     time.sleep(dt)
                 ids.append(srv.submit(rq))
-            sts = [srv.wait(i, 900_000) for i in ids]
+            sts = [srv.wait(i, 1_800_000) for i in ids]
             wall = time.perf_counter() - t0
             stats = srv.stats()
-        return reqs, sts, wall, stats
+        try:
+            engine = json.loads(Path(log_path).read_text().strip().splitlines()[-1])
+        except (OSError, ValueError, IndexError):
+            engine = {}
+        Path(log_path).unlink(missing_ok=True)
+        return reqs, sts, wall, stats, engine
 
-    reqs1, sts1, wall1, stats1 = run([0.0] * len(items))
+    ncap = min(args.serve_capacity_requests, len(items))
+    reqs1, sts1, wall1, stats1, _ = run(range(ncap), [0.0] * ncap)
     its = sum(s["pixel_iters"] for s in sts1)
-    rate = args.serve_load * len(items) / wall1
-    gaps = np.array([it.gap for it in items]) / rate
+    rate = args.serve_load * ncap / wall1
+    n = args.serve_requests
+    gaps = np.array([it.gap for it in items[:n]]) / rate
     arrivals = np.cumsum(gaps) - gaps[0]
-    reqs2, sts2, wall2, stats2 = run(list(arrivals))
-    same = all(np.array_equal(a.counts, b.counts) for a, b in zip(reqs1, reqs2))
+    reqs2, sts2, wall2, stats2, engine = run(range(n), list(arrivals))
+    same = all(np.array_equal(a.counts, b.counts) for a, b in zip(reqs1, reqs2[:ncap]))
     lat = np.array([s["latency_ms"] for s in sts2])
     ok = all(s["state"] == "done" for s in sts1 + sts2)
-    methods = {"perturbation": sum(1 for s in sts2 if s["method"] == 1),
-               "multi_limb": sum(1 for s in sts2 if s["method"] == 2)}
+    sizes = np.array([f"{it.width}x{it.height}" for it in items[:n]])
+    meth = np.array(["perturbation" if s["method"] == 1 else "multi_limb" for s in sts2])
+    busy = stats2["busy_ms"]
+    dev = engine.get("device_step_ms")
     return {
-        "requests": len(items), "seed": args.serve_seed, "all_done": ok,
+        "requests": n, "seed": args.serve_seed, "all_done": ok,
         "stream": "sizes {240x180..1920x1080}, log2 span U[-1000,-10], prec ceil(-log2 span)+64, "
                   "mandelbrot/burning ship/celtic 0.7/0.2/0.1, maxiter log-U[1e3,1e5]",
-        "capacity_run_s": wall1,
-        "throughput": {"value": its / wall1, "unit": "pixel-iters/s",
-                       "note": "closed loop, all requests submitted at once, through the "
-                               "public submit/wait API with host result buffers"},
+        "capacity": {"requests": ncap, "run_s": wall1,
+                     "throughput": {"value": its / wall1, "unit": "pixel-iters/s"},
+                     "note": "closed loop, all requests submitted at once, through the public "
+                             "submit/wait API with host result buffers"},
         "poisson_rate_per_s": rate, "load": args.serve_load, "poisson_run_s": wall2,
-        "latency_ms": {"p50": float(np.percentile(lat, 50, method="inverted_cdf")),
-                       "p99": float(np.percentile(lat, 99, method="inverted_cdf")),
-                       "max": float(lat.max()), "mean": float(lat.mean())},
+        "latency_ms": latency_summary(lat),
+        "latency_ms_by_size": {k: latency_summary(lat[sizes == k]) for k in sorted(set(sizes))},
+        "latency_ms_by_method": {k: latency_summary(lat[meth == k]) for k in sorted(set(meth))},
         "results_equal_across_runs": same,
         "steps": stats2["steps"], "gpu_launches": stats2["launches"],
-        "device_bytes_peak": stats2["device_bytes_peak"], "methods": methods,
+        "step_loop": {"host_ms": busy, "device_ms": dev,
+                      "host_share_above_device": (1.0 - dev / busy) if dev and busy else None,
+                      "graph_launch_ms": engine.get("loop_ms", {}).get("graph_launch")},
+        "device_bytes_peak": stats2["device_bytes_peak"],
     }
 
 

@@ -1,8 +1,9 @@
 """Builds libmdzgpu.so (sm_103a) in-tree with nvcc.
 
 Every translation unit under mdz_gb300/csrc is compiled in parallel into
-mdz_gb300/_build/, the multi-limb kernel once per word count listed in
-csrc/internal.h (MDZ_MP_WORDS_LIST), and linked into mdz_gb300/lib/.
+mdz_gb300/_build/, the multi-limb kernels once per word count listed in
+csrc/internal.h (MDZ_MP_WORDS_LIST, MDZ_MPW_LIST), and linked into
+mdz_gb300/lib/.
 Objects are rebuilt when their source or any csrc header is newer.
 """
 from __future__ import annotations
@@ -42,12 +43,25 @@ def mp_word_counts() -> list[int]:
     return [int(x) for x in re.findall(r"X\((\d+)\)", m.group(1))]
 
 
+def mpw_configs() -> list[tuple[int, int, int]]:
+    text = (CSRC / "internal.h").read_text()
+    m = re.search(r"#define MDZ_MPW_LIST\(X\)((?:.*\\\n)*.*)", text)
+    if not m:
+        raise RuntimeError("MDZ_MPW_LIST not found")
+    return [tuple(int(v) for v in t) for t in
+            re.findall(r"X\((\d+),\s*(\d+),\s*(\d+)\)", m.group(1))]
+
+
 def _jobs() -> list[tuple[Path, Path, list[str]]]:
     jobs = []
     for src in sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp")):
         if src.name == "mp_kernel.cu":
             for n in mp_word_counts():
                 jobs.append((src, BUILD / f"mp_kernel_w{n}.o", [f"-DMDZ_MP_WORDS={n}"]))
+        elif src.name == "mpw_kernel.cu":
+            for n, g, q in mpw_configs():
+                jobs.append((src, BUILD / f"mpw_kernel_w{n}.o",
+                             [f"-DMDZ_MPW_G={g}", f"-DMDZ_MPW_Q={q}"]))
         else:
             jobs.append((src, BUILD / (src.stem + ".o"), []))
     return jobs

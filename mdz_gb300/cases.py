@@ -10,7 +10,8 @@ perturbation frame (orbit + FP32 pixels + escalation passes); serve: the
 first requests of the seeded serving stream through the serving engine;
 ship: the burning-ship perturbation on the 2^-300 view of the folded-formula
 fixtures (tests/golden/perturb_fold_views.json, f_ship_a300).
---frame keeps the view's pixel spacing and crops around its centre.
+--frame keeps the view's pixel spacing and crops around its centre; --depth
+overrides the view's maxiter (shorter reference orbits for profiling).
 Prints one JSON line of the call's statistics per repeat.
 """
 from __future__ import annotations
@@ -45,6 +46,7 @@ def main(argv=None) -> None:
     ap.add_argument("--aa", action="store_true")
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--requests", type=int, default=4)
+    ap.add_argument("--depth", type=int, default=0, help="maxiter override (0: the view's)")
     a = ap.parse_args(argv)
     if a.case == "serve":
         from .serve import Server
@@ -72,6 +74,8 @@ def main(argv=None) -> None:
                 print(json.dumps(st), flush=True)
         return
     v = view(a.case, a.frame, a.aa)
+    if a.depth:
+        v.depth = a.depth
     with Renderer(0) as r:
         for _ in range(a.repeat):
             if a.case in ("c1", "c2"):

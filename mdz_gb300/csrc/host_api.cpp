@@ -350,7 +350,13 @@ int mdzgpu_render_fp64_device(mdzgpu_ctx* ctx, const mdzgpu_frame* f, double xmi
 
 int32_t mdzgpu_mp_max_words(void)
 {
-    return 36;
+    int w = kMpThreadMaxWords;
+#define MDZ_CASE(n, g, q) \
+    if (n > w)            \
+        w = n;
+    MDZ_MPW_LIST(MDZ_CASE)
+#undef MDZ_CASE
+    return w;
 }
 
 static int pick_words(long precision, int words)
@@ -568,7 +574,7 @@ OrbitLayout orbit_layout(size_t entries, int L)
 {
     // zq[entries] float4 | zd[entries] double2 | ze[entries] int |
     // dd[entries] double | de[entries] int | tiny bits | fm[entries] double |
-    // fe[entries] int | axis bits | len + progress words |
+    // fe[entries] int | axis bits | attention bits | len + progress words |
     // centre digits | rebases | digits[entries][2][L] int (raw orbit, scratch)
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     OrbitLayout o;
@@ -580,7 +586,8 @@ OrbitLayout orbit_layout(size_t entries, int L)
     o.fm = o.tiny + al((entries / 32 + 40) * sizeof(unsigned));  // + whole last batches
     o.fe = o.fm + al(entries * sizeof(double));
     o.axis = o.fe + al(entries * sizeof(int));
-    o.len = o.axis + al((entries / 32 + 40) * sizeof(unsigned));
+    o.att = o.axis + al((entries / 32 + 40) * sizeof(unsigned));
+    o.len = o.att + al((entries / 32 + 40) * sizeof(unsigned));
     o.dig = o.len + 256;
     o.reb = o.dig + al(2 * (size_t)L * sizeof(int));
     o.raw = o.reb + 256;
@@ -797,6 +804,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     o.fm = (double*)(ob + ol.fm);
     o.fe = (int*)(ob + ol.fe);
     o.axis = (unsigned*)(ob + ol.axis);
+    o.att = (unsigned*)(ob + ol.att);
     o.spin_limit = ctx->wait_limit;
     OrbitLaunch oq = o;   // Julia: the critical orbit; hybrid: the even-step one
     if (two) {
@@ -821,6 +829,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         oq.fe = o.fe + q0;
         oq.tiny = o.tiny + q0 / 32;
         oq.axis = o.axis + q0 / 32;
+        oq.att = o.att + q0 / 32;
         oq.out_len = o.out_len + 16;   // beside V's length, in the zeroed progress block
     }
     int64_t h2d_extra = 0;
@@ -880,6 +889,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.de = o.de;
     p.orbit_len = o.out_len;
     p.tiny = o.tiny;
+    p.att = o.att;
     p.fractal = f->fractal;
     p.fm = o.fm;
     p.fe = o.fe;

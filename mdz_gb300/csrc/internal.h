@@ -154,8 +154,21 @@ bool mp_words_supported(int words);
 // Word counts the multi-limb kernel is compiled for (one translation unit
 // each; the build reads this list).
 #define MDZ_MP_WORDS_LIST(X) X(4) X(6) X(8) X(10) X(12) X(16) X(20) X(24) X(28) X(34) X(36)
+// Word counts beyond one thread's registers: the warp-cooperative kernel
+// (mpw_kernel.cu), as (words, lanes per pixel G, 64-bit limbs per lane Q)
+// with words = 2 G Q (one translation unit each; the build reads this list).
+#define MDZ_MPW_LIST(X) \
+    X(48, 8, 3) X(64, 8, 4) X(80, 8, 5) X(96, 8, 6) X(128, 16, 4) X(160, 16, 5) X(192, 16, 6) \
+    X(256, 32, 4)
+// Largest word count of the one-thread kernel (and of the serving engine's
+// multi-limb slice kernels).
+constexpr int kMpThreadMaxWords = 36;
 template <int N>
 int launch_words(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
+template <int G, int Q>
+int launch_wide(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s);
+template <int G, int Q>
+int preload_wide();
 template <int N>
 int preload_words();
 // Loads (and sets up) every multi-limb frame kernel / every perturbation
@@ -180,6 +193,9 @@ struct OrbitLaunch {
     int* sm_busy = nullptr; // serving: producers per SM id (counted while running)
     int sm_words = 0;
     unsigned* tiny = nullptr;  // [max_k / 32 + 2] bit k: |Z_k|^2 < 2^-120 (FP32)
+    // [max_k / 32 + 2] bit k: |Z_k|^2 > 4 - 2^-14 or < 2^-60 in FP32 (the
+    // entries where the FP32 pixel step needs a test)
+    unsigned* att = nullptr;
     // formula: MDZ_MANDELBROT, MDZ_BURNING_SHIP (Im = 2 |Re Im| + Ci) or
     // MDZ_GENERALIZED_CELTIC (Re = |Re^2 - Im^2| + Cr)
     int fractal = 0;
@@ -225,6 +241,7 @@ struct PerturbLaunch {
     const int* de;
     const int* orbit_len;   // device: valid orbit entries
     const unsigned* tiny;   // bit mask of tiny |Z_k| (see OrbitLaunch)
+    const unsigned* att = nullptr;  // attention bit mask (see OrbitLaunch); null: unused
     int fractal = 0;        // MDZ_MANDELBROT / _BURNING_SHIP / _GENERALIZED_CELTIC
     const double* fm = nullptr;  // fold quantity F_k = fm * 2^fe (see OrbitLaunch)
     const int* fe = nullptr;
@@ -310,7 +327,7 @@ int mpfr_round_to_fixed(const mdzgpu_mpval* v, long p, int words, uint32_t* out)
 // Reference-orbit buffer: byte offsets of its 256-byte aligned pieces for
 // `entries` entries of L digits (zf at 0).
 struct OrbitLayout {
-    size_t zd, ze, dd, de, tiny, fm, fe, axis, len, dig, reb, raw, bytes;
+    size_t zd, ze, dd, de, tiny, fm, fe, axis, att, len, dig, reb, raw, bytes;
 };
 OrbitLayout orbit_layout(size_t entries, int L);
 // Multi-limb word count of the perturbation's last escalation pass.

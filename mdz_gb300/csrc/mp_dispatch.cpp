@@ -11,6 +11,11 @@ bool mp_words_supported(int words)
         return true;
     MDZ_MP_WORDS_LIST(MDZ_CASE)
 #undef MDZ_CASE
+#define MDZ_CASE(n, g, q) \
+    if (words == n)       \
+        return true;
+    MDZ_MPW_LIST(MDZ_CASE)
+#undef MDZ_CASE
     return false;
 }
 
@@ -21,6 +26,11 @@ int launch_mp(mdzgpu_ctx* ctx, const MpLaunch& p, cudaStream_t s)
     case n:         \
         return launch_words<n>(ctx, p, s);
         MDZ_MP_WORDS_LIST(MDZ_CASE)
+#undef MDZ_CASE
+#define MDZ_CASE(n, g, q) \
+    case n:               \
+        return launch_wide<g, q>(ctx, p, s);
+        MDZ_MPW_LIST(MDZ_CASE)
 #undef MDZ_CASE
     default:
         set_error("mp kernel: %d words not built", p.words);
@@ -35,6 +45,11 @@ int preload_mp_kernels()
     if (!rc)                     \
         rc = preload_words<n>();
     MDZ_MP_WORDS_LIST(MDZ_CASE)
+#undef MDZ_CASE
+#define MDZ_CASE(n, g, q)           \
+    if (!rc)                        \
+        rc = preload_wide<g, q>();
+    MDZ_MPW_LIST(MDZ_CASE)
 #undef MDZ_CASE
     return rc;
 }

@@ -43,7 +43,7 @@ namespace {
 constexpr int kTileW = 8;
 constexpr int kTileH = 4;
 constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
-constexpr int kOrbitThreads = 128;  // producer threads (four warps)
+constexpr int kOrbitThreads = 512;  // producer threads (sixteen warps)
 
 // --------------------------------------------------------------------------
 // Reference orbit
@@ -115,200 +115,227 @@ __device__ __forceinline__ int digits_sign_warp(const int2* z, int L, bool imag)
     return 0;
 }
 
-// The producer, run by kOrbitThreads = 128 threads (threadIdx.x < 128) with
-// named barrier 1: warp w computes part w & 1 (0: Re, 1: Im) over half
-// w >> 1 of every column's terms; the second halves' partial sums meet the
-// first halves' in shared memory, whose warps then resolve the carries and
-// write Z_{k+1}.  Publishes raw_len every 32 steps when `prog` is given.
-// Inlined into each kernel that runs it, so that each has its own register
-// budget: as one shared function it spilled in the loop (the fused
-// kernel's bound applied to all callers).  Splitting the columns over eight
-// warps instead of four measured 3% slower (more partial sums per step).
+// The producer, run by every thread of its block (NT = blockDim.x, a
+// multiple of 32, >= 64).  One step Z_k -> Z_{k+1} in two phases:
+//
+//  1. Products.  The L + 3 kept columns c = L-4 .. 2L-2 (3 guard columns
+//     below the L digits of the result) are split into S term slices each;
+//     the (column, slice) items are spread over all threads, so a thread
+//     forms at most a few digit pairs (i < j = c - i, i = lo + s + S t) of
+//     both parts at once: Re = sum x_i x_j - y_i y_j, Im = sum x_i y_j +
+//     x_j y_i, one pair of 64-bit loads feeding four IMAD.WIDE.  Slice 0 adds
+//     the square term of an even column.  Partial sums go to shared memory.
+//  2. Carries.  Warp 0 (Re) and warp 1 (Im) add the S partials of their
+//     columns (one column per lane and 32-column slot), apply the formula's
+//     sign rules, add C, and resolve the carries in two warp-shuffle passes,
+//     which leave every digit within 2^27 + 2^5 of zero, small enough for
+//     the next products' 64-bit column sums; they write Z_{k+1} to shared
+//     memory and its digits to HBM, and the FP32 top-digit estimate (escape
+//     test) and, for burning ship, the part's sign.
+//
+// The column sums are exact integers, so the result does not depend on how
+// the terms are sliced (any NT gives the same digits).  The escape test of
+// Z_k is evaluated while Z_{k+1}'s products are formed: a step computed past
+// an escape is dropped (nothing of it reaches HBM before the test).
+// Everything else about each Z_k (FP64 / FP32 roundings, |Z_k|^2 - 4) is
+// done afterwards by the finisher, in parallel over k.  Publishes raw_len
+// every 64 steps when `prog` is given.  Inlined into each kernel that runs
+// it, so that each has its own register budget.
+constexpr int kOrbitMaxSlices = 8;
+constexpr int kOrbitMaxCols = kMaxOrbitLimbs + 3;
+
+struct OrbitShared {
+    int2 z[kMaxOrbitLimbs];                              // Z_k digit pairs (re, im)
+    int cc[2][kMaxOrbitLimbs];                           // C digits
+    long long part[2][kOrbitMaxSlices][kOrbitMaxCols];   // [Re/Im][slice][column]
+    float esc[2][2];   // [Re/Im][k & 1]: top two digits of Z_k as FP32
+    int sgn[2][2];     // [Re/Im][k & 1]: sign of the part of Z_k (burning ship)
+};
+
+// Top-digit estimate and (burning ship) sign of one part of the Z just
+// written to o.z, by the carry warp of that part (all lanes).
+__device__ __forceinline__ void orbit_part_summary(OrbitShared& o, int L, int part, int slot,
+                                                   bool ship)
+{
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) {
+        const int2 t1 = o.z[L - 1], t2 = o.z[L - 2];
+        o.esc[part][slot] = part ? fmaf((float)t2.y, 3.7252903e-9f, (float)t1.y)
+                                 : fmaf((float)t2.x, 3.7252903e-9f, (float)t1.x);
+    }
+    if (ship) {
+        const int sg = digits_sign_warp(o.z, L, part == 1);
+        if ((threadIdx.x & 31) == 0)
+            o.sgn[part][slot] = sg;
+    }
+}
+
 __device__ __forceinline__ void orbit_produce(const OrbitLaunch& p, const OrbitProgress* prog)
 {
-    __shared__ int2 z[kMaxOrbitLimbs];
-    __shared__ int cc[2][kMaxOrbitLimbs];
-    __shared__ long long partial[2][3][32];
-    auto bar = [] { asm volatile("bar.sync 1, 128;" ::: "memory"); };
+    __shared__ OrbitShared o;
+    const int NT = blockDim.x;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int part = warp & 1;   // 0: real, 1: imaginary
-    const int half = warp >> 1;  // which half of each column's terms
     const int L = p.limbs;
+    const int P = L + 3;           // kept columns cbase .. cbase + P - 1
+    const int cbase = L - 4;       // lowest column computed (3 guard columns)
+    const int nslots = (P + 31) / 32;
+    int S = NT / P;
+    S = S < 1 ? 1 : (S > kOrbitMaxSlices ? kOrbitMaxSlices : S);
     const bool from_z0 = p.z0_re != nullptr;   // Julia: Z_0 given, k starts at 0
-    for (int j = threadIdx.x; j < L; j += kOrbitThreads) {
-        cc[0][j] = p.c_re[j];
-        cc[1][j] = p.c_im[j];
+    const bool ship = p.fractal == MDZ_BURNING_SHIP;
+    const bool celtic = p.fractal == MDZ_GENERALIZED_CELTIC;
+    const bool variant = p.fractal == MDZ_VARIANT;
+    for (int j = threadIdx.x; j < L; j += NT) {
+        o.cc[0][j] = p.c_re[j];
+        o.cc[1][j] = p.c_im[j];
         if (from_z0) {
-            z[j] = make_int2(p.z0_re[j], p.z0_im[j]);
+            o.z[j] = make_int2(p.z0_re[j], p.z0_im[j]);
             p.digits[j] = p.z0_re[j];
             p.digits[L + j] = p.z0_im[j];
         } else {
-            z[j] = make_int2(p.c_re[j], p.c_im[j]);
+            o.z[j] = make_int2(p.c_re[j], p.c_im[j]);
             p.digits[j] = 0;                    // Z_0 = 0
             p.digits[L + j] = 0;
             p.digits[2 * L + j] = p.c_re[j];    // Z_1 = C
             p.digits[3 * L + j] = p.c_im[j];
         }
     }
-    const int cbase = L - 4;       // lowest column computed (3 guard columns)
-    const int ctop = 2 * L - 2;    // highest column
-    const int nslots = (ctop - cbase + 32) / 32;
-    const int* cpart = cc[part];
-    const bool ship = p.fractal == MDZ_BURNING_SHIP;
-    const bool celtic = p.fractal == MDZ_GENERALIZED_CELTIC;
-    const bool variant = p.fractal == MDZ_VARIANT;
+    __threadfence();
+    __syncthreads();
     int k = from_z0 ? 0 : 1;
+    if (warp < 2)
+        orbit_part_summary(o, L, warp, k & 1, ship);
     for (;; ++k) {
-        if (prog && (k & 31) == 0) {
-            __threadfence();  // this thread's digits of Z_0..Z_k
-            bar();
-            if (threadIdx.x == 0)
-                *(volatile int*)prog->raw_len = k + 1;
-        }
-        bar();  // Z_k complete in shared memory
-        // escape test on the two top digits, evaluated by every thread
-        // (FP32 is enough to stop the orbit: stopping a step early or late
-        // only moves a rebase)
-        {
-            const int2 t1 = z[L - 1], t2 = z[L - 2];
-            const float a = (float)t1.x + (float)t2.x * 3.7252903e-9f;
-            const float b = (float)t1.y + (float)t2.y * 3.7252903e-9f;
-            if (a * a + b * b > 4.0f || k >= p.max_k)
-                break;
-        }
-        // celtic fold of this step (every step, or the variant's odd ones)
-        const bool fold_re = celtic || (variant && (k & 1) == p.fold_parity);
-        // burning ship: Im' = 2 |Re| |Im| + Ci = sign(Re) sign(Im) 2 Re Im + Ci
-        const int sxy = ship ? digits_sign_warp(z, L, false) * digits_sign_warp(z, L, true) : 1;
-        long long v[3] = {0, 0, 0};
-#pragma unroll
-        for (int s = 0; s < 3; ++s) {
-            const int c = cbase + lane + 32 * s;
-            if (s >= nslots || c > ctop)
-                continue;
+        __syncthreads();  // A: Z_k, its estimate and signs complete
+        if (prog && (k & 63) == 0 && threadIdx.x == 0)
+            *(volatile int*)prog->raw_len = k + 1;
+        // phase 1: partial column sums of Z_k^2
+        for (int q = threadIdx.x; q < S * P; q += NT) {
+            const int s = q / P;
+            const int pos = q - s * P;
+            const int c = cbase + pos;
             const int lo = c - (L - 1) > 0 ? c - (L - 1) : 0;
-            const int hi = (c - 1) >> 1;  // i < j = c - i
-            const int mid = lo + (hi - lo + 2) / 2;
-            int i = half ? mid : lo;
-            const int ihi = half ? hi : mid - 1;
-            long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-            if (part == 0) {
-                for (; i + 3 <= ihi; i += 4) {
-                    const int j = c - i;
-                    const int2 p0 = z[i], q0 = z[j], p1 = z[i + 1], q1 = z[j - 1];
-                    const int2 p2 = z[i + 2], q2 = z[j - 2], p3 = z[i + 3], q3 = z[j - 3];
-                    a0 += (long long)p0.x * q0.x - (long long)p0.y * q0.y;
-                    a1 += (long long)p1.x * q1.x - (long long)p1.y * q1.y;
-                    a2 += (long long)p2.x * q2.x - (long long)p2.y * q2.y;
-                    a3 += (long long)p3.x * q3.x - (long long)p3.y * q3.y;
-                }
-                for (; i <= ihi; ++i) {
-                    const int2 pi = z[i], qj = z[c - i];
-                    a0 += (long long)pi.x * qj.x - (long long)pi.y * qj.y;
-                }
-            } else {
-                for (; i + 3 <= ihi; i += 4) {
-                    const int j = c - i;
-                    const int2 p0 = z[i], q0 = z[j], p1 = z[i + 1], q1 = z[j - 1];
-                    const int2 p2 = z[i + 2], q2 = z[j - 2], p3 = z[i + 3], q3 = z[j - 3];
-                    a0 += (long long)p0.x * q0.y + (long long)q0.x * p0.y;
-                    a1 += (long long)p1.x * q1.y + (long long)q1.x * p1.y;
-                    a2 += (long long)p2.x * q2.y + (long long)q2.x * p2.y;
-                    a3 += (long long)p3.x * q3.y + (long long)q3.x * p3.y;
-                }
-                for (; i <= ihi; ++i) {
-                    const int2 pi = z[i], qj = z[c - i];
-                    a0 += (long long)pi.x * qj.y + (long long)qj.x * pi.y;
-                }
+            const int hi = (c - 1) >> 1;  // last i with i < j = c - i
+            long long r0 = 0, r1 = 0, m0 = 0, m1 = 0;
+            int i = lo + s;
+            for (; i + S <= hi; i += 2 * S) {
+                const int2 a = o.z[i], b = o.z[c - i];
+                const int2 a2 = o.z[i + S], b2 = o.z[c - i - S];
+                r0 += (long long)a.x * b.x - (long long)a.y * b.y;
+                m0 += (long long)a.x * b.y + (long long)b.x * a.y;
+                r1 += (long long)a2.x * b2.x - (long long)a2.y * b2.y;
+                m1 += (long long)a2.x * b2.y + (long long)b2.x * a2.y;
             }
-            long long acc = 2 * ((a0 + a1) + (a2 + a3));
-            if (!half && !(c & 1)) {
-                const int2 h = z[c >> 1];
-                acc += part == 0 ? (long long)h.x * h.x - (long long)h.y * h.y
-                                 : 2 * (long long)h.x * h.y;
+            if (i <= hi) {
+                const int2 a = o.z[i], b = o.z[c - i];
+                r0 += (long long)a.x * b.x - (long long)a.y * b.y;
+                m0 += (long long)a.x * b.y + (long long)b.x * a.y;
             }
-            if (part == 1)
-                acc *= sxy;
-            // celtic adds Cr after the fold (below)
-            if (!half && c >= L - 1 && !(fold_re && part == 0))
-                acc += cpart[c - (L - 1)];
-            v[s] = acc;
+            long long re = 2 * (r0 + r1), im = 2 * (m0 + m1);
+            if (s == 0 && !(c & 1)) {
+                const int2 h = o.z[c >> 1];
+                re += (long long)h.x * h.x - (long long)h.y * h.y;
+                im += 2 * (long long)h.x * h.y;
+            }
+            o.part[0][s][pos] = re;
+            o.part[1][s][pos] = im;
         }
-        if (half) {
-#pragma unroll
-            for (int s = 0; s < 3; ++s)
-                partial[part][s][lane] = v[s];
-        }
-        bar();  // partial sums in place; every read of Z_k done
-        if (half)
+        const float ea = o.esc[0][k & 1], eb = o.esc[1][k & 1];
+        const bool stop = fmaf(ea, ea, eb * eb) > 4.0f || k >= p.max_k;
+        const int sxy = ship ? o.sgn[0][k & 1] * o.sgn[1][k & 1] : 1;
+        __syncthreads();  // B: partial sums in place; every read of Z_k done
+        if (stop)
+            break;
+        if (warp >= 2)
             continue;
+        // phase 2 (warp 0: Re, warp 1: Im): Z_{k+1}
+        const int part = warp;
+        // celtic fold of this step (every step, or the variant's odd ones)
+        const bool fold_re = part == 0 && (celtic || (variant && (k & 1) == p.fold_parity));
+        long long v[3];
 #pragma unroll
-        for (int s = 0; s < 3; ++s)
-            v[s] += partial[part][s][lane];
-        // carry propagation: column c+1 is lane+1 (slot s) or lane 0 of
-        // slot s+1; two passes bound every digit by 2^27 + 2^5
+        for (int t = 0; t < 3; ++t) {
+            const int pos = lane + 32 * t;
+            long long acc = 0;
+            if (t < nslots && pos < P) {
+                for (int s = 0; s < S; ++s)
+                    acc += o.part[part][s][pos];
+                // burning ship: Im' = 2 |Re| |Im| + Ci = sign(Re) sign(Im) 2 Re Im + Ci
+                if (part == 1)
+                    acc *= sxy;
+                // celtic adds Cr after the fold (below)
+                if (pos >= 3 && !fold_re)
+                    acc += o.cc[part][pos - 3];
+            }
+            v[t] = acc;
+        }
+        // carry propagation: column pos+1 is lane+1 (slot t) or lane 0 of
+        // slot t+1; two passes bound every digit by 2^27 + 2^5
         auto carry2 = [&]() {
 #pragma unroll
             for (int pass = 0; pass < 2; ++pass) {
                 long long dg[3], cy[3];
 #pragma unroll
-                for (int s = 0; s < 3; ++s)
-                    digit_split(v[s], dg[s], cy[s]);
+                for (int t = 0; t < 3; ++t)
+                    digit_split(v[t], dg[t], cy[t]);
 #pragma unroll
-                for (int s = 0; s < 3; ++s) {
-                    if (s >= nslots)
+                for (int t = 0; t < 3; ++t) {
+                    if (t >= nslots)
                         break;
-                    long long in = __shfl_up_sync(0xffffffffu, cy[s], 1);
+                    long long in = __shfl_up_sync(0xffffffffu, cy[t], 1);
                     const long long wrap =
-                        __shfl_sync(0xffffffffu, s > 0 ? cy[s - 1] : 0ll, 31);
+                        __shfl_sync(0xffffffffu, t > 0 ? cy[t - 1] : 0ll, 31);
                     if (lane == 0)
                         in = wrap;
-                    v[s] = dg[s] + in;
+                    v[t] = dg[t] + in;
                 }
             }
         };
         carry2();
-        if (fold_re && part == 0) {
+        if (fold_re) {
             // Re' = |Re^2 - Im^2| + Cr: the sign of the carried digits is
             // that of their most significant nonzero one
             int sg = 0;
 #pragma unroll
-            for (int s = 2; s >= 0; --s) {
-                const int c = cbase + lane + 32 * s;
-                const bool ok = s < nslots && c <= ctop && v[s] != 0;
+            for (int t = 2; t >= 0; --t) {
+                const int pos = lane + 32 * t;
+                const bool ok = t < nslots && pos < P && v[t] != 0;
                 const unsigned m = __ballot_sync(0xffffffffu, ok);
                 if (m && !sg) {
-                    const long long t = __shfl_sync(0xffffffffu, v[s], 31 - __clz(m));
-                    sg = t > 0 ? 1 : -1;
+                    const long long x = __shfl_sync(0xffffffffu, v[t], 31 - __clz(m));
+                    sg = x > 0 ? 1 : -1;
                 }
             }
 #pragma unroll
-            for (int s = 0; s < 3; ++s) {
-                const int c = cbase + lane + 32 * s;
+            for (int t = 0; t < 3; ++t) {
+                const int pos = lane + 32 * t;
                 if (sg < 0)
-                    v[s] = -v[s];
-                if (s < nslots && c <= ctop && c >= L - 1)
-                    v[s] += cpart[c - (L - 1)];
+                    v[t] = -v[t];
+                if (t < nslots && pos < P && pos >= 3)
+                    v[t] += o.cc[0][pos - 3];
             }
             carry2();
         }
         int* out = p.digits + (size_t)(k + 1) * 2 * L + part * L;
 #pragma unroll
-        for (int s = 0; s < 3; ++s) {
-            const int c = cbase + lane + 32 * s;
-            if (s < nslots && c <= ctop && c >= L - 1) {
-                const int d = (int)v[s];
+        for (int t = 0; t < 3; ++t) {
+            const int pos = lane + 32 * t;
+            if (t < nslots && pos < P && pos >= 3) {
+                const int d = (int)v[t];
                 if (part == 0)
-                    z[c - (L - 1)].x = d;
+                    o.z[pos - 3].x = d;
                 else
-                    z[c - (L - 1)].y = d;
-                out[c - (L - 1)] = d;
+                    o.z[pos - 3].y = d;
+                out[pos - 3] = d;
             }
         }
+        orbit_part_summary(o, L, part, (k + 1) & 1, ship);
+        if (prog && ((k + 1) & 63) == 0)
+            __threadfence();  // Z_{k+1}'s digits before raw_len = k + 2
     }
     __threadfence();
-    bar();
+    __syncthreads();
     if (threadIdx.x == 0) {
         *p.out_len = k + 1;  // entries 0..k are valid
         if (prog) {
@@ -451,25 +478,34 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
 }
 
 // Bit k of p.tiny: |Z_k|^2 < 2^-120 in FP32 (the pixel pass takes the full
-// floatexp step there when dz is below the FP32 range); bit k of p.axis:
+// floatexp step there when dz is below the FP32 range); bit k of p.att:
+// |Z_k|^2 in the FP32 escape band or below the rebase screen's 2^-60 (a
+// superset of tiny: the deep-zoom blocks skip their tests where it is
+// clear); bit k of p.axis:
 // |F_k| < 2^-99 (burning ship / celtic: a dz of the FP32 range can carry a
 // pixel across the fold there).  Written per warp of 32 consecutive
 // entries, so every word has one writer.
 __device__ __forceinline__ void write_tiny_bits(const OrbitLaunch& p, int k, bool valid)
 {
-    bool tiny = false, axis = false;
+    bool tiny = false, axis = false, att = false;
     if (valid) {
-        tiny = p.zq[k].z < 7.5e-37f;
+        const float m2 = p.zq[k].z;
+        tiny = m2 < 7.5e-37f;
+        // as the FP32 pixel loop tests |z|^2 = |Z_k|^2 (Mant<float>)
+        att = m2 > 4.0f - 6.1035156e-5f || m2 < 8.7e-19f;
         if (p.fm)
             axis = p.fm[k] == 0.0 || p.fe[k] <= -99;
     }
     const unsigned bits = __ballot_sync(0xffffffffu, tiny);
     const unsigned abits = __ballot_sync(0xffffffffu, axis);
+    const unsigned tbits = __ballot_sync(0xffffffffu, att);
     if ((threadIdx.x & 31) == 0 && k >= 0) {
         if (p.tiny)
             p.tiny[k >> 5] = bits;
         if (p.axis)
             p.axis[k >> 5] = abits;
+        if (p.att)
+            p.att[k >> 5] = tbits;
     }
 }
 
@@ -482,10 +518,11 @@ __global__ void __launch_bounds__(128) orbit_finish_kernel(OrbitLaunch p)
     write_tiny_bits(p, k, valid);
 }
 
-// The finisher of the streamed orbit (one block of 256 threads): finishes
-// the orbit in batches of 256 entries as the producer publishes them and
-// publishes fin_len in units of 1024 entries, so a consumer never reads a
-// cache line holding an unfinished entry.
+// The finisher of the streamed orbit (one block of B = blockDim.x threads, a
+// multiple of 32 dividing 1024): finishes the orbit in batches of B entries
+// as the producer publishes them and publishes fin_len in units of 1024
+// entries, so a consumer never reads a cache line holding an unfinished
+// entry.
 __device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
 {
     __shared__ int s_avail, s_done, s_err;
@@ -496,7 +533,7 @@ __device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
             for (;;) {
                 d = *(volatile int*)g.done;
                 r = d ? *(volatile int*)p.out_len : *(volatile int*)g.raw_len;
-                if (d || r >= fin + 256)
+                if (d || r >= fin + (int)blockDim.x)
                     break;
                 if (*(volatile int*)g.error || ++spins > p.spin_limit) {
                     err = 1;
@@ -515,7 +552,7 @@ __device__ void orbit_finisher(const OrbitLaunch& p, const OrbitProgress& g)
                 atomicExch(g.error, 1);
             return;
         }
-        const int end = min(avail, fin + 256);
+        const int end = min(avail, fin + (int)blockDim.x);
         const int k = fin + (int)threadIdx.x;
         if (k < end)
             finish_entry(p, k, true);
@@ -676,8 +713,13 @@ __device__ __forceinline__ void slow_step(const PerturbLaunch& p, int m, PixStat
 
 // |z|^2 > 4 decided from D_m = |Z_m|^2 - 4 (exact, from the orbit digits):
 // |z|^2 - 4 = D_m + 2 Re(conj(Z_m) dz) + |dz|^2, in FP64 with exponents.
+// The deltas themselves carry the rounding error of the steps since the last
+// rebase, about sqrt(n) 2^-24 of |dz| after n steps; `unsure` is set when
+// the margin is within 4 2^-14 (|Z| |dz| + |dz|^2) of zero (2^-14 covers
+// 10^6 steps at that rate): the decision then goes to the next pass.
 template <class T>
-__device__ __forceinline__ bool escape_exact(const PerturbLaunch& p, int m, const PixState<T>& st)
+__device__ __forceinline__ bool escape_exact(const PerturbLaunch& p, int m, const PixState<T>& st,
+                                             bool& unsure)
 {
     const double2 zd = p.zd[m];
     const int ze = p.ze[m];
@@ -689,6 +731,10 @@ __device__ __forceinline__ bool escape_exact(const PerturbLaunch& p, int m, cons
     const int e3 = 2 * st.e;
     const int E = max(max(dexp_of(dd) + de, dexp_of(t2) + e2), dexp_of(t3) + e3);
     const double v = ldexp(dd, de - E) + ldexp(t2, e2 - E) + ldexp(t3, e3 - E);
+    // in units of 2^E, as v
+    const double zm = sqrt(zd.x * zd.x + zd.y * zd.y), dm = sqrt(t3);
+    const double err = 2.44140625e-4 * (ldexp(zm * dm, e2 - E) + ldexp(t3, e3 - E));
+    unsure = !(fabs(v) > err);
     return v > 0.0;
 }
 
@@ -702,11 +748,20 @@ __device__ __forceinline__ bool z_tiny(const PerturbLaunch& p, int m, T zx, T zy
     return zx * zx + zy * zy < (T)Mant<T>::kTinyZ2;
 }
 
-// True when none of Z_m .. Z_{m+3} is tiny (FP32 bit mask).  The next word
+// five_clear: bits m .. m+4 of a bit mask are all clear (the attention mask
+// of the deep-zoom blocks).
+// four_not_tiny: none of Z_m .. Z_{m+3} is tiny (FP32 bit mask).  The next word
 // is read only when bits m .. m+3 reach into it: a word holding no entry
 // below the orbit progress must not be loaded (the finisher publishes whole
 // 128-byte lines of the mask, and a line loaded early would stay stale in
 // this SM's L1 for the rest of the launch).
+__device__ __forceinline__ bool five_clear(const unsigned* mask, int m)
+{
+    const unsigned lo = __ldg(mask + (m >> 5));
+    const unsigned hi = ((unsigned)m & 31u) > 27u ? __ldg(mask + (m >> 5) + 1) : 0u;
+    return (__funnelshift_r(lo, hi, (unsigned)m & 31u) & 0x1fu) == 0u;
+}
+
 __device__ __forceinline__ bool four_not_tiny(const PerturbLaunch& p, int m)
 {
     const unsigned lo = __ldg(p.tiny + (m >> 5));
@@ -1260,6 +1315,46 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                    && m + 4 < avail && !st.force_slow
                    && (!st.slow_if_tiny || four_not_tiny(p, m))) {
             // iterations wz .. wz+3, orbit entries m+1 .. m+4 all finished
+            if (st.s == (T)0 && p.att && five_clear(p.att, m)) {
+                // deep zoom and none of Z_m .. Z_{m+4} needs attention
+                // (escape band, rebase screen, tiny |Z|): whole blocks of
+                // four run with no test inside, their four orbit loads issued
+                // together; the values are those of the checked block below
+                // (the checks it makes would all have passed)
+                do {
+                    const float4 q1 = p.zq[m + 1], q2 = p.zq[m + 2], q3 = p.zq[m + 3],
+                                 q4 = p.zq[m + 4];
+                    const T zx[4] = {Zx, (T)q1.x, (T)q2.x, (T)q3.x};
+                    const T zy[4] = {Zy, (T)q1.y, (T)q2.y, (T)q3.y};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const T tr = st.tr, ti = st.ti;
+                        const T u2 = tr + tr, v2 = ti + ti;
+                        st.tr = Mant<T>::fma_(zx[u], u2, Mant<T>::fma_(-zy[u], v2, st.dcr));
+                        st.ti = Mant<T>::fma_(zx[u], v2, Mant<T>::fma_(zy[u], u2, st.dci));
+                    }
+                    Zx = (T)q4.x;
+                    Zy = (T)q4.y;
+                    magT = (T)q4.z;
+                    m += 4;
+                    wz += 4;
+                    // wz - 1 = 4k + 4: the rescale check of the general path
+                    const T amax = fmax(fabs(st.tr), fabs(st.ti));
+                    if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
+                        const int k = Mant<T>::exponent_of(amax);
+                        const T sc = Mant<T>::scale((T)1, -k);
+                        st.tr *= sc;
+                        st.ti *= sc;
+                        st.e += k;
+                        refresh_scale(st, dcf_r, dcf_i, dce);
+                    }
+                } while (st.s == (T)0 && !st.force_slow && wz + 3u <= last && m + 4 < avail
+                         && five_clear(p.att, m));
+                // as a resumed pixel computes it
+                zr = Mant<T>::fma_(st.s, st.tr, Zx);
+                zi = Mant<T>::fma_(st.s, st.ti, Zy);
+                continue;
+            }
             if (st.s == (T)0) {
                 // dz below the FP32 range (deep zoom): s t and s t^2 vanish
                 // exactly, so the step is t' = 2 Z_m t + dc 2^-e, |z|^2 is
@@ -1404,8 +1499,14 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 }
             }
         } else if (magT > band_lo) {
-            // within 2^-14 of the bailout the rounded Z_m can not decide it
-            if (magT > band_hi || escape_exact<T>(p, m, st)) {
+            // within 2^-14 of the bailout the rounded Z_m can not decide it;
+            // where the deltas' own error could decide it either way the
+            // pixel is re-run by the FP64 pass (which tracks that error)
+            bool unsure = false;
+            const bool esc = magT > band_hi || escape_exact<T>(p, m, st, unsure);
+            if (unsure)
+                r.lost = fmaxf(r.lost, 64.f);
+            if (esc) {
                 r.mag = (float)magT;
                 count = wz;
                 return 1;
@@ -1607,7 +1708,7 @@ __global__ void __launch_bounds__(256) perturb_kernel(PerturbLaunch p)
     }
 }
 
-// One cooperative launch: block 0 produces the reference orbit (64
+// One cooperative launch: block 0 produces the reference orbit (all its
 // threads), block 1 finishes its entries, every other block iterates pixels
 // (FP32 pass) as soon as the entries they need are finished.  Pixel work per
 // orbit step is larger than the producer's, so the orbit's serial time hides
@@ -1622,8 +1723,7 @@ __global__ void __launch_bounds__(256, 5) perturb_fused_kernel(OrbitLaunch o, Pe
         if (threadIdx.x == 0)
             *(volatile int*)p.producer_sm = (int)smid + 1;
         OrbitProgress g{p.raw_len, p.fin_len, p.orbit_done, p.orbit_error};
-        if (threadIdx.x < kOrbitThreads)
-            orbit_produce(o, &g);
+        orbit_produce(o, &g);
         return;
     }
     if (blockIdx.x == 1) {
@@ -1776,10 +1876,10 @@ __global__ void __launch_bounds__(256, FR == MDZ_MANDELBROT ? 5 : 4)
 
 // ---- streamed orbit: pixels start while the orbit is being iterated ----
 
-// Block 0: the producer (128 threads); block 1: the finisher.  Launched
-// cooperatively (both blocks resident at once: the finisher waits, bounded,
-// on the producer's progress).
-__global__ void __launch_bounds__(256) orbit_stream_kernel(OrbitLaunch o, OrbitProgress g,
+// Block 0: the producer (kOrbitThreads threads); block 1: the finisher.
+// Launched cooperatively (both blocks resident at once: the finisher waits,
+// bounded, on the producer's progress).
+__global__ void __launch_bounds__(kOrbitThreads) orbit_stream_kernel(OrbitLaunch o, OrbitProgress g,
                                                            int* producer_sm, DoneSignal done)
 {
     if (blockIdx.x == 0) {
@@ -1790,8 +1890,7 @@ __global__ void __launch_bounds__(256) orbit_stream_kernel(OrbitLaunch o, OrbitP
                 atomicAdd(o.sm_busy + smid % (unsigned)o.sm_words, 1);
             *(volatile int*)producer_sm = (int)smid + 1;
         }
-        if (threadIdx.x < kOrbitThreads)
-            orbit_produce(o, &g);
+        orbit_produce(o, &g);
         if (threadIdx.x == 0) {
             *(volatile int*)producer_sm = 0;
             if (o.sm_busy)
@@ -1995,8 +2094,8 @@ int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s, Don
     OrbitProgress g{progress + 1, progress + 2, progress + 3, progress + 4};
     int* producer_sm = progress + 5;
     void* args[] = {&oo, &g, &producer_sm, &done};
-    MDZ_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)orbit_stream_kernel, dim3(2), dim3(256),
-                                             args, 0, s));
+    MDZ_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)orbit_stream_kernel, dim3(2),
+                                             dim3(kOrbitThreads), args, 0, s));
     return MDZGPU_OK;
 }
 

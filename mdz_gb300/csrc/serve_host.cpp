@@ -267,9 +267,9 @@ int prepare(const mdzgpu_request* q, Req& r)
     r.timeout_ms = q->timeout_ms;
     const int w_need = mp_words_for_precision(r.precision);
     r.words = perturb_mp_words(r.precision);
-    if (method == MDZGPU_METHOD_MULTI_LIMB && w_need > mdzgpu_mp_max_words()) {
-        set_error("serve: precision %ld needs %d words, the multi-limb kernel has %d",
-                  r.precision, w_need, mdzgpu_mp_max_words());
+    if (method == MDZGPU_METHOD_MULTI_LIMB && w_need > kMpThreadMaxWords) {
+        set_error("serve: precision %ld needs %d words, the multi-limb slice kernel has %d",
+                  r.precision, w_need, kMpThreadMaxWords);
         return MDZGPU_ERR_UNSUPPORTED;
     }
     if (method == MDZGPU_METHOD_PERTURB) {
@@ -735,6 +735,7 @@ int Server::setup(const std::shared_ptr<Req>& r)
         p.de = (const int*)(ob + ol.de);
         p.orbit_len = (const int*)(ob + ol.len);
         p.tiny = (const unsigned*)(ob + ol.tiny);
+        p.att = (const unsigned*)(ob + ol.att);
         p.fractal = r->fractal;
         p.fm = (const double*)(ob + ol.fm);
         p.fe = (const int*)(ob + ol.fe);
@@ -765,6 +766,7 @@ int Server::setup(const std::shared_ptr<Req>& r)
         o.max_k = (int)r->depth + 1;
         o.out_len = (int*)(ob + ol.len);
         o.tiny = (unsigned*)(ob + ol.tiny);
+        o.att = (unsigned*)(ob + ol.att);
         o.fractal = r->fractal;
         o.fm = (double*)(ob + ol.fm);
         o.fe = (int*)(ob + ol.fe);

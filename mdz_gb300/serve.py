@@ -69,6 +69,45 @@ class RenderRequest:
         return r
 
 
+def request_from_view(v, method: str = "auto", want_mag: bool = False,
+                      timeout_ms: float = 0.0) -> RenderRequest:
+    """A serving request for an MDZ view (mdz_gb300.View, e.g. from a
+    settings file): its centre, depth, precision, formula, family and Julia
+    constant, over its real (supersampled) pixels.  MDZ's `size` is the
+    real-axis width of a wide frame and the imaginary-axis height of a tall
+    one (src/coords.c:265-302); the request takes the real-axis span."""
+    from fractions import Fraction
+
+    from .mpval import parse_number
+    prec = max(int(v.precision), 64)
+    W, H = v.real_width, v.real_height
+    size = parse_number(v.size)
+    aspect = Fraction(v.width / v.height)        # a double, as MDZ computes it
+    span = size if aspect > 1 else size * aspect
+    julia = None
+    if v.family == 1:
+        julia = (MpVal.from_fraction(parse_number(v.julia_re), prec),
+                 MpVal.from_fraction(parse_number(v.julia_im), prec))
+    return RenderRequest(W, H, int(v.depth), MpVal.from_fraction(parse_number(v.cx), prec),
+                         MpVal.from_fraction(parse_number(v.cy), prec),
+                         MpVal.from_fraction(span, prec), prec, fractal=int(v.fractal),
+                         method=method, want_mag=want_mag, family=int(v.family), julia=julia,
+                         timeout_ms=timeout_ms)
+
+
+def request_from_mdz(path, width: int = 0, height: int = 0, aa: int = 0,
+                     intended: bool = False, **kw) -> RenderRequest:
+    """A serving request for an MDZ settings file (.mdz): the view MDZ's
+    headless render takes from it (image_info_load_settings,
+    src/image_info.c:456-721; `mdz -s file -W w -H h -a aa`).  MDZ renders a
+    rectangle-form file around the rectangle's centre at size 4.0;
+    `intended=True` takes the file's own rectangle instead."""
+    from . import mdzfile
+    s = mdzfile.load(path)
+    v = s.intended_view(width, height, aa) if intended else s.view(width, height, aa)
+    return request_from_view(v, **kw)
+
+
 def footprint(req: RenderRequest) -> tuple[int, int]:
     """(device bytes, pinned host bytes) the request holds while admitted."""
     lib = native.load()

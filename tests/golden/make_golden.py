@@ -12,6 +12,8 @@ reference sources exist; the GPU tests only read the committed outputs).
   python tests/golden/make_golden.py perturb_julia # perturb_julia.npz (Julia family, MPFR 2p)
   python tests/golden/make_golden.py perturb_variant  # perturb_variant.npz (hybrid, MPFR 2p)
   python tests/golden/make_golden.py c2        # c2_frame.json + c2_rows.npz (full config-2 frame)
+  python tests/golden/make_golden.py serve_mdz # mdz/*.mdz + serve_mdz.npz (settings files served)
+  python tests/golden/make_golden.py perturb_rebase  # perturb_rebase.npz (2^-1000, rebases at depth)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -119,6 +121,50 @@ def make_c2() -> None:
     np.savez_compressed(GOLD / "c2_rows.npz", rows=rows)
     (GOLD / "c2_frame.json").write_text(json.dumps(meta, indent=1))
     print(f"c2: {ref.shape} iters={meta['pixel_iters']} ({time.time() - t0:.1f}s)")
+
+
+def make_serve_mdz() -> None:
+    """The reference's gallery settings files, written out again by
+    mdz_gb300.mdzfile.dumps into tests/golden/mdz/ (the loader reads them
+    back to the same settings), and for each the serving request the
+    settings-file path builds (64 pixels across, the file's own rectangle)
+    with MPFR at p and 2p bits on every pixel of the serving geometry."""
+    from mdz_gb300 import mdzfile, perturb_pixel_c
+    from mdz_gb300.serve import request_from_mdz
+    dst = GOLD / "mdz"
+    dst.mkdir(exist_ok=True)
+    out, meta = {}, {}
+    for f in sorted(_gallery().glob("*.mdz")):
+        try:
+            s = mdzfile.load(f)
+        except mdzfile.MdzFileError as e:
+            print(f"{f.name}: skipped ({e})")
+            continue
+        path = dst / f.name
+        path.write_text(mdzfile.dumps(s))
+        back = mdzfile.load(path)
+        assert back.intended_view(64).__dict__ == s.intended_view(64).__dict__, f.name
+        req = request_from_mdz(path, width=64, intended=True)
+        W, H, prec = req.width, req.height, req.precision
+        t0 = time.time()
+        cre, cim = [], []
+        for ln in range(H):
+            for ix in range(W):
+                x, y = perturb_pixel_c(req.cx, req.cy, req.span, W, H, ix, ln)
+                cre.append(hexfloat(x))
+                cim.append(hexfloat(y))
+        c1, _ = O.points_mpfr(cre, cim, req.depth, prec, fractal=req.fractal, threads=THREADS)
+        c2, _ = O.points_mpfr(cre, cim, req.depth, 2 * prec, fractal=req.fractal,
+                              threads=THREADS)
+        key = f.stem
+        out[key] = c2.reshape(H, W).astype(np.int32)
+        out[key + "__p"] = c1.reshape(H, W).astype(np.int32)
+        meta[key] = dict(file=f"mdz/{f.name}", W=W, H=H, depth=req.depth, prec=prec,
+                         fractal=req.fractal, oracle_prec=2 * prec)
+        print(f"{key}: {W}x{H} depth {req.depth} prec {prec} fractal {req.fractal} "
+              f"confirmed {(c1 == c2).mean():.4f} ({time.time() - t0:.1f}s)")
+    np.savez_compressed(GOLD / "serve_mdz.npz", **out)
+    (GOLD / "serve_mdz.json").write_text(json.dumps(meta, indent=1))
 
 
 # --------------------------------------------------------------------------
@@ -518,6 +564,38 @@ def make_perturb() -> None:
     (GOLD / "perturb_views.json").write_text(json.dumps(meta, indent=1))
 
 
+def make_perturb_rebase() -> None:
+    """A 2^-1000 frame whose reference orbit ends long before maxiter: the
+    centre is the seeded ray-bisection boundary point at depth 120000
+    (seed 9, refined to 1088 bits), rendered to depth 200000, so every pixel
+    still running when the reference escapes rebases onto Z_0 and carries on
+    with deltas of order one.  Scored, as config 4, on 4096 seeded pixels
+    against MPFR at 2176 bits (counts and |z|^2 at escape)."""
+    t0 = time.time()
+    cx, cy = bisect_mpfr(seed=9, depth=120000, prec=1088)
+    print(f"rebase view centre: {time.time() - t0:.1f}s")
+    W, H, depth, width = 1920, 1080, 200000, Fraction(2) ** -1000
+    rng = np.random.Generator(np.random.PCG64(9009))
+    ix = rng.integers(0, W, 4096)
+    ln = rng.integers(0, H, 4096)
+    cre, cim = [], []
+    for a, b in zip(ix, ln):
+        x, y = perturb_c(cx, cy, width, W, H, int(a), int(b))
+        cre.append(hexfloat(x))
+        cim.append(hexfloat(y))
+    t0 = time.time()
+    counts, mag = O.points_mpfr(cre, cim, depth, 2176, threads=THREADS)
+    ref_count, _ = O.points_mpfr([hexfloat(cx)], [hexfloat(cy)], depth, 2176)
+    print(f"rebase view samples at 2176 bits: {time.time() - t0:.1f}s; centre escapes at "
+          f"{int(ref_count[0])}; samples escaping: {(counts > 0).mean():.3f}")
+    np.savez_compressed(GOLD / "perturb_rebase.npz", ix=ix.astype(np.int32),
+                        line=ln.astype(np.int32), counts=counts.astype(np.int64), mag=mag)
+    (GOLD / "perturb_rebase.json").write_text(json.dumps(dict(
+        cx=hexfloat(cx), cy=hexfloat(cy), width=hexfloat(width), W=W, H=H, depth=depth,
+        prec=1088, oracle_prec=2176, samples=4096, seed=9009, bisect_seed=9,
+        bisect_depth=120000, centre_count=int(ref_count[0])), indent=1))
+
+
 def make_perturb_fold() -> None:
     """Burning ship and celtic frames for the folded perturbation, scored
     against MPFR at twice the precision.  The deep views sit at the serving
@@ -722,7 +800,8 @@ def main(argv: list[str]) -> None:
         {"fp64": make_fp64, "views": make_views, "abi": make_abi, "mp": make_mp,
          "perturb": make_perturb, "centres": make_centres, "colour": make_colour,
          "perturb_fold": make_perturb_fold, "perturb_julia": make_perturb_julia,
-         "perturb_variant": make_perturb_variant, "c2": make_c2}[w]()
+         "perturb_variant": make_perturb_variant, "c2": make_c2,
+         "serve_mdz": make_serve_mdz, "perturb_rebase": make_perturb_rebase}[w]()
 
 
 if __name__ == "__main__":

@@ -32,11 +32,12 @@ def test_footprint_perturbation_layout():
     entries = 5002
     orbit = (al(entries * 16) + al(entries * 16) + al(entries * 4) + al(entries * 8)
              + al(entries * 4) + al((entries // 32 + 40) * 4) + al(entries * 8)
-             + al(entries * 4) + al((entries // 32 + 40) * 4) + 256 + al(2 * L * 4) + 256
-             + al(entries * 2 * L * 4))
+             + al(entries * 4) + al((entries // 32 + 40) * 4) + al((entries // 32 + 40) * 4)
+             + 256 + al(2 * L * 4) + 256 + al(entries * 2 * L * 4))
     # counts, |z|^2, 32-byte pixel state, two escalation lists, sync, orbit
     # (zq, zd, ze, dd, de, tiny-|Z| bit mask, fold value fm / fe, fold-axis
-    # bit mask, progress, centre, rebases, raw digits), escalation-pass
+    # bit mask, attention bit mask, progress, centre, rebases, raw digits),
+    # escalation-pass
     # coordinates
     words = 12   # 300 + 40 bits -> 11 words -> even
     expect = (al(4 * n) + al(4 * n) + al(32 * n) + al(256 + 8 * n) + 256 + al(orbit)
