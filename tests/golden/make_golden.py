@@ -564,17 +564,76 @@ def make_perturb() -> None:
     (GOLD / "perturb_views.json").write_text(json.dumps(meta, indent=1))
 
 
+def _fx_log2_abs2(re: int, im: int, F: int) -> float:
+    """log2 |x + iy|^2 of fixed-point integers (F fractional bits); -inf at 0."""
+    a = re * re + im * im
+    if a == 0:
+        return -math.inf
+    sh = max(0, a.bit_length() - 60)
+    return math.log2(a >> sh) + sh - 2 * F
+
+
+def find_nucleus(cx: Fraction, cy: Fraction, radius: Fraction, maxp: int,
+                 F: int = 1120) -> tuple[int, Fraction, Fraction]:
+    """The nucleus of a minibrot near c0 = cx + i cy: its period p is the
+    first n whose first-order image of the disc |c - c0| < radius,
+    Z_n + dZ_n/dc (c - c0), contains 0; the nucleus solves Z_p(c) = 0 by
+    Newton's method from c0 (Python integers, F fractional bits)."""
+    one = 1 << F
+    CR, CI = int(cx * one), int(cy * one)
+    zr = zi = dr = di = 0
+    lr2 = 2 * (math.log2(radius.numerator) - math.log2(radius.denominator))
+    p = 0
+    for n in range(1, maxp + 1):
+        # dZ' = 2 Z dZ + 1, Z' = Z^2 + C
+        dr, di = ((2 * (zr * dr - zi * di)) >> F) + one, (2 * (zr * di + zi * dr)) >> F
+        zr, zi = ((zr * zr - zi * zi) >> F) + CR, ((2 * zr * zi) >> F) + CI
+        lz2 = _fx_log2_abs2(zr, zi, F)
+        if lz2 > 2.0:
+            raise RuntimeError(f"centre escapes at {n}")
+        if lz2 < lr2 + _fx_log2_abs2(dr, di, F):
+            p = n
+            break
+    if not p:
+        raise RuntimeError("no period below maxp")
+    cr, ci = CR, CI
+    for _ in range(60):
+        zr = zi = dr = di = 0
+        for _ in range(p):
+            dr, di = ((2 * (zr * dr - zi * di)) >> F) + one, (2 * (zr * di + zi * dr)) >> F
+            zr, zi = ((zr * zr - zi * zi) >> F) + cr, ((2 * zr * zi) >> F) + ci
+        den = dr * dr + di * di
+        if den == 0:
+            raise RuntimeError("zero derivative")
+        # (zr + i zi) / (dr + i di) in units of 2^-F
+        qr = ((zr * dr + zi * di) << F) // den
+        qi = ((zi * dr - zr * di) << F) // den
+        cr, ci = cr - qr, ci - qi
+        if abs(qr) <= 4 and abs(qi) <= 4:
+            break
+    return p, Fraction(cr, one), Fraction(ci, one)
+
+
 def make_perturb_rebase() -> None:
-    """A 2^-1000 frame whose reference orbit ends long before maxiter: the
-    centre is the seeded ray-bisection boundary point at depth 120000
-    (seed 9, refined to 1088 bits), rendered to depth 200000, so every pixel
-    still running when the reference escapes rebases onto Z_0 and carries on
-    with deltas of order one.  Scored, as config 4, on 4096 seeded pixels
-    against MPFR at 2176 bits (counts and |z|^2 at escape)."""
-    t0 = time.time()
-    cx, cy = bisect_mpfr(seed=9, depth=120000, prec=1088)
-    print(f"rebase view centre: {time.time() - t0:.1f}s")
+    """A 2^-1000 frame, maxiter 200000, whose reference orbit passes through
+    zero: the view is centred on the nucleus of a minibrot near the
+    Misiurewicz point c = i whose size is about the frame's (its period p
+    from the first-order image of a disc of radius 2^-500 around i, the
+    nucleus by Newton's method), so Z_p is ~0 and every pixel rebases there
+    (|Z_p + dz| < |dz|) -- and again at every multiple of p it reaches --
+    while the pixels near the cardioid's edge orbit for up to ~2*10^5
+    iterations before escaping.  The reference never escapes.  Scored, as
+    config 4, on 4096 seeded pixels against MPFR at 2176 bits (counts and
+    |z|^2 at escape).  (Around config 4's own centre the dynamics are nearly
+    parabolic -- |dZ/dc| only reaches ~2^137 by iteration 200000 -- so a
+    2^-1000 frame there is flat: every pixel escapes within one iteration of
+    the reference and no pixel rebases.)"""
     W, H, depth, width = 1920, 1080, 200000, Fraction(2) ** -1000
+    t0 = time.time()
+    p, cx, cy = find_nucleus(Fraction(0), Fraction(1), Fraction(2) ** -500, 20000, F=1200)
+    cx = MpVal.from_fraction(cx, 1088).to_fraction()
+    cy = MpVal.from_fraction(cy, 1088).to_fraction()
+    print(f"nucleus of period {p} ({time.time() - t0:.1f}s)")
     rng = np.random.Generator(np.random.PCG64(9009))
     ix = rng.integers(0, W, 4096)
     ln = rng.integers(0, H, 4096)
@@ -585,15 +644,14 @@ def make_perturb_rebase() -> None:
         cim.append(hexfloat(y))
     t0 = time.time()
     counts, mag = O.points_mpfr(cre, cim, depth, 2176, threads=THREADS)
-    ref_count, _ = O.points_mpfr([hexfloat(cx)], [hexfloat(cy)], depth, 2176)
-    print(f"rebase view samples at 2176 bits: {time.time() - t0:.1f}s; centre escapes at "
-          f"{int(ref_count[0])}; samples escaping: {(counts > 0).mean():.3f}")
+    print(f"rebase view samples at 2176 bits: {time.time() - t0:.1f}s; counts "
+          f"{int(counts.min())}..{int(counts.max())}, {len(np.unique(counts))} distinct, "
+          f"{(counts == 0).mean():.3f} not escaping")
     np.savez_compressed(GOLD / "perturb_rebase.npz", ix=ix.astype(np.int32),
                         line=ln.astype(np.int32), counts=counts.astype(np.int64), mag=mag)
     (GOLD / "perturb_rebase.json").write_text(json.dumps(dict(
         cx=hexfloat(cx), cy=hexfloat(cy), width=hexfloat(width), W=W, H=H, depth=depth,
-        prec=1088, oracle_prec=2176, samples=4096, seed=9009, bisect_seed=9,
-        bisect_depth=120000, centre_count=int(ref_count[0])), indent=1))
+        prec=1088, oracle_prec=2176, samples=4096, seed=9009, period=p), indent=1))
 
 
 def make_perturb_fold() -> None:

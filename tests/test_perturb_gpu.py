@@ -81,6 +81,42 @@ def test_perturb_config4_samples(renderer):
     assert frac <= 0.001, f"{frac:.5f} of the 4096 samples differ"
 
 
+def test_perturb_rebase_view_samples(renderer):
+    """A 2^-1000 frame (1920x1080, maxiter 200000) centred on the nucleus of
+    a minibrot whose cardioid spans the frame: the reference orbit passes
+    through zero once a period, so pixels rebase there again and again
+    (Zhuoran's rebasing, |Z_m + dz| < |dz|) while the ones near the
+    cardioid's edge orbit for up to ~2*10^5 iterations before escaping.
+    Scored on 4096 seeded pixels against MPFR at 2176 bits."""
+    path = GOLD / "perturb_rebase.json"
+    if not path.exists():
+        pytest.skip("fixture not generated")
+    m = json.loads(path.read_text())
+    data = np.load(GOLD / "perturb_rebase.npz")
+    prec = m["prec"]
+    cx = MpVal.from_fraction(parse_number(m["cx"]), prec)
+    cy = MpVal.from_fraction(parse_number(m["cy"]), prec)
+    w = MpVal.from_fraction(parse_number(m["width"]), prec)
+    counts, mag, st = renderer.render_perturb(m["W"], m["H"], m["depth"], cx, cy, w, prec,
+                                              want_mag=True)
+    ix, ln = data["ix"], data["line"]
+    got = counts[ln, ix].astype(np.int64)
+    want = data["counts"]
+    diff = got != want
+    ok = (~diff) & (want > 0)
+    err = np.abs(smooth(got[ok], mag[ln, ix][ok].astype(np.float64))
+                 - smooth(want[ok], data["mag"][ok]))
+    print(f"rebase view: {int(diff.sum())}/4096 samples differ "
+          f"(max count error {int(np.abs(got - want).max())}); smooth-colour error p99 "
+          f"{np.nanpercentile(err, 99):.2e} max {np.nanmax(err):.2e}; rebases {st['rebases']}; "
+          f"escalated fp64 {st['escalated_fp64']} mp {st['escalated_mp']}; "
+          f"{st['kernel_ms']:.0f} ms")
+    assert st["rebases"] > 0
+    assert int(want.max()) > 100000
+    assert float(diff.mean()) <= 0.001, f"{int(diff.sum())} of the 4096 samples differ"
+    assert float(np.nanpercentile(err, 99)) < 0.01
+
+
 @pytest.mark.parametrize("cx,cy,prec,n", [("-0.75", "0.1", 128, 60),
                                           ("0x1p-40", "1", 320, 100),
                                           ("-1.7497856353511106873", "0.0000153218", 1088, 200)])
