@@ -381,7 +381,14 @@ def run_serving(args, local) -> dict:
         "steps": stats2["steps"], "gpu_launches": stats2["launches"],
         "step_loop": {"host_ms": busy, "device_ms": dev,
                       "host_share_above_device": (1.0 - dev / busy) if dev and busy else None,
-                      "graph_launch_ms": engine.get("loop_ms", {}).get("graph_launch")},
+                      "graph_launch_ms": engine.get("loop_ms", {}).get("graph_launch"),
+                      "step_gap_ms": engine.get("step_gap_ms"),
+                      "fixed_overhead_share": (engine["step_gap_ms"]["p10"] * stats2["steps"] / dev)
+                      if dev and engine.get("step_gap_ms") else None,
+                      "note": "per step, host wall (graph launch to sync) minus the step's device "
+                              "span; its 10th percentile (steps not held up behind other "
+                              "kernels) times the step count, over the device time, is the fixed "
+                              "launch-and-sync overhead"},
         "device_bytes_peak": stats2["device_bytes_peak"],
     }
 

@@ -42,6 +42,16 @@ namespace {
 
 constexpr int kTileW = 8;
 constexpr int kTileH = 4;
+// A pixel of the FP32 pass that rebases more often than this is re-run by
+// the FP64 pass.  Repeated rebases mean its orbit keeps returning to the
+// reference's zero -- a pixel around a minibrot, where the count can hinge
+// on the position of c to far below 2^-24 of its offset (near the edge of
+// the minibrot's cardioid the escape time grows like 1/sqrt(distance)), and
+// the FP32 steps' rounding, equivalent to moving c by ~2^-24 |dc| a step,
+// then shifts it by iterations to thousands of iterations (measured on a
+// 2^-1000 frame centred on a period-402 nucleus: 1.2% of the pixels wrong
+// in FP32, none once re-run in FP64).
+constexpr unsigned kFp32RebaseLimit = 8;
 constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
 constexpr int kOrbitThreads = 512;  // producer threads (sixteen warps)
 
@@ -346,10 +356,237 @@ __device__ __forceinline__ void orbit_produce(const OrbitLaunch& p, const OrbitP
     }
 }
 
-__global__ void __launch_bounds__(kOrbitThreads) orbit_kernel(OrbitLaunch p)
+// The producer of the standalone orbit kernels (orbit_kernel,
+// orbit_stream_kernel), with every thread's work fixed before the loop.
+// Same column sums and carries as orbit_produce, so the same digits; laid
+// out for the shortest serial step: the kept columns are split into
+// kOrbitLeanSlices term slices, and thread q < slices x columns owns one
+// (slice, column) item whose at most MAXP digit pairs are known before the
+// first step (shared-memory indices, padded with a zero entry, so every
+// thread runs the same straight-line code); warps 0 and 1 then add the
+// slices' partial sums of their columns (NSLOT per lane), add C, fold and
+// resolve the carries as orbit_produce does.  The generic loop spent most
+// of its serial step on per-step index arithmetic (divisions, variable trip
+// counts); orbit_produce stays for the fused launch, whose blocks are
+// smaller than slices x columns.
+constexpr int kOrbitLeanSlices = 8;
+
+template <int MAXP, int NSLOT>
+__device__ __forceinline__ void orbit_produce_lean(const OrbitLaunch& p, const OrbitProgress* prog)
 {
-    // serving: the slice kernels keep their blocks off an SM while a
-    // producer runs there, so its latency-bound warps own the issue slots
+    constexpr int S = kOrbitLeanSlices;
+    __shared__ int2 z[kMaxOrbitLimbs + 1];                  // z[L] stays zero
+    __shared__ int cc[2][kMaxOrbitLimbs];
+    __shared__ long long part[2][S][kMaxOrbitLimbs + 3];
+    __shared__ float esc[2][2];
+    __shared__ int sgn[2][2];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int L = p.limbs;
+    const int P = L + 3;
+    const int cbase = L - 4;
+    const bool from_z0 = p.z0_re != nullptr;
+    const bool ship = p.fractal == MDZ_BURNING_SHIP;
+    const bool celtic = p.fractal == MDZ_GENERALIZED_CELTIC;
+    const bool variant = p.fractal == MDZ_VARIANT;
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        cc[0][j] = p.c_re[j];
+        cc[1][j] = p.c_im[j];
+        if (from_z0) {
+            z[j] = make_int2(p.z0_re[j], p.z0_im[j]);
+            p.digits[j] = p.z0_re[j];
+            p.digits[L + j] = p.z0_im[j];
+        } else {
+            z[j] = make_int2(p.c_re[j], p.c_im[j]);
+            p.digits[j] = 0;                    // Z_0 = 0
+            p.digits[L + j] = 0;
+            p.digits[2 * L + j] = p.c_re[j];    // Z_1 = C
+            p.digits[3 * L + j] = p.c_im[j];
+        }
+    }
+    if (threadIdx.x == 0)
+        z[L] = make_int2(0, 0);
+    // this thread's item and its pair indices
+    const int q = threadIdx.x;
+    const bool worker = q < S * P;
+    const int s = worker ? q / P : 0;
+    const int pos = worker ? q - s * P : 0;
+    const int c = cbase + pos;
+    const int lo = c - (L - 1) > 0 ? c - (L - 1) : 0;
+    const int hi = (c - 1) >> 1;
+    int ia[MAXP], ib[MAXP];
+#pragma unroll
+    for (int j = 0; j < MAXP; ++j) {
+        const int i = lo + s + S * j;
+        const bool ok = worker && i <= hi;
+        ia[j] = ok ? i : L;
+        ib[j] = ok ? c - i : L;
+    }
+    const int ih = (worker && s == 0 && !(c & 1)) ? (c >> 1) : L;
+    __threadfence();
+    __syncthreads();
+    int k = from_z0 ? 0 : 1;
+    // top-digit estimate (escape test) and, for burning ship, the sign of
+    // part pt of the Z just written (all lanes of warp pt)
+    auto summary = [&](int pt, int slot) {
+        __syncwarp();
+        if (lane == 0) {
+            const int2 t1 = z[L - 1], t2 = z[L - 2];
+            esc[pt][slot] = pt ? fmaf((float)t2.y, 3.7252903e-9f, (float)t1.y)
+                               : fmaf((float)t2.x, 3.7252903e-9f, (float)t1.x);
+        }
+        if (ship) {
+            const int sg = digits_sign_warp(z, L, pt == 1);
+            if (lane == 0)
+                sgn[pt][slot] = sg;
+        }
+    };
+    if (warp < 2)
+        summary(warp, k & 1);
+    for (;; ++k) {
+        __syncthreads();  // A: Z_k, its estimate and signs complete
+        if (prog && (k & 63) == 0 && threadIdx.x == 0)
+            *(volatile int*)prog->raw_len = k + 1;
+        if (worker) {
+            long long r0 = 0, r1 = 0, m0 = 0, m1 = 0;
+#pragma unroll
+            for (int j = 0; j < MAXP; ++j) {
+                const int2 a = z[ia[j]], b = z[ib[j]];
+                if (j & 1) {
+                    r1 += (long long)a.x * b.x;
+                    r1 -= (long long)a.y * b.y;
+                    m1 += (long long)a.x * b.y;
+                    m1 += (long long)b.x * a.y;
+                } else {
+                    r0 += (long long)a.x * b.x;
+                    r0 -= (long long)a.y * b.y;
+                    m0 += (long long)a.x * b.y;
+                    m0 += (long long)b.x * a.y;
+                }
+            }
+            const int2 h = z[ih];
+            long long re = 2 * (r0 + r1), im = 2 * (m0 + m1);
+            re += (long long)h.x * h.x;
+            re -= (long long)h.y * h.y;
+            im += 2 * ((long long)h.x * h.y);
+            part[0][s][pos] = re;
+            part[1][s][pos] = im;
+        }
+        const float ea = esc[0][k & 1], eb = esc[1][k & 1];
+        const bool stop = fmaf(ea, ea, eb * eb) > 4.0f || k >= p.max_k;
+        const int sxy = ship ? sgn[0][k & 1] * sgn[1][k & 1] : 1;
+        __syncthreads();  // B: partial sums in place; every read of Z_k done
+        if (stop)
+            break;
+        if (warp >= 2)
+            continue;
+        // Z_{k+1}: warp 0 the real part, warp 1 the imaginary part
+        const int pt = warp;
+        const bool fold_re = pt == 0 && (celtic || (variant && (k & 1) == p.fold_parity));
+        long long v[NSLOT];
+#pragma unroll
+        for (int t = 0; t < NSLOT; ++t) {
+            const int pp = lane + 32 * t;
+            long long a = 0;
+            if (pp < P) {
+                long long u[S];
+#pragma unroll
+                for (int ss = 0; ss < S; ++ss)
+                    u[ss] = part[pt][ss][pp];
+                a = ((u[0] + u[1]) + (u[2] + u[3])) + ((u[4] + u[5]) + (u[6] + u[7]));
+                if (pt == 1)
+                    a *= sxy;
+                if (pp >= 3 && !fold_re)
+                    a += cc[pt][pp - 3];
+            }
+            v[t] = a;
+        }
+        auto carry2 = [&]() {
+#pragma unroll
+            for (int pass = 0; pass < 2; ++pass) {
+                long long dg[NSLOT], cy[NSLOT];
+#pragma unroll
+                for (int t = 0; t < NSLOT; ++t)
+                    digit_split(v[t], dg[t], cy[t]);
+#pragma unroll
+                for (int t = 0; t < NSLOT; ++t) {
+                    long long in = __shfl_up_sync(0xffffffffu, cy[t], 1);
+                    const long long wrap =
+                        __shfl_sync(0xffffffffu, t > 0 ? cy[t - 1] : 0ll, 31);
+                    if (lane == 0)
+                        in = wrap;
+                    v[t] = dg[t] + in;
+                }
+            }
+        };
+        carry2();
+        if (fold_re) {
+            int sg = 0;
+#pragma unroll
+            for (int t = NSLOT - 1; t >= 0; --t) {
+                const int pp = lane + 32 * t;
+                const bool ok = pp < P && v[t] != 0;
+                const unsigned m = __ballot_sync(0xffffffffu, ok);
+                if (m && !sg) {
+                    const long long x = __shfl_sync(0xffffffffu, v[t], 31 - __clz(m));
+                    sg = x > 0 ? 1 : -1;
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < NSLOT; ++t) {
+                const int pp = lane + 32 * t;
+                if (sg < 0)
+                    v[t] = -v[t];
+                if (pp < P && pp >= 3)
+                    v[t] += cc[0][pp - 3];
+            }
+            carry2();
+        }
+        int* out = p.digits + (size_t)(k + 1) * 2 * L + pt * L;
+#pragma unroll
+        for (int t = 0; t < NSLOT; ++t) {
+            const int pp = lane + 32 * t;
+            if (pp >= 3 && pp < P) {
+                const int d = (int)v[t];
+                if (pt == 0)
+                    z[pp - 3].x = d;
+                else
+                    z[pp - 3].y = d;
+                out[pp - 3] = d;
+            }
+        }
+        summary(pt, (k + 1) & 1);
+        if (prog && ((k + 1) & 63) == 0)
+            __threadfence();  // Z_{k+1}'s digits before raw_len = k + 2
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *p.out_len = k + 1;  // entries 0..k are valid
+        if (prog) {
+            *(volatile int*)prog->raw_len = k + 1;
+            __threadfence();
+            *(volatile int*)prog->done = 1;
+        }
+    }
+}
+
+// (MAXP, NSLOT) of the lean producer for L digits: a column holds at most
+// floor(L / 2) pairs, spread over 8 slices; L + 3 columns over 32 lanes.
+#define MDZ_ORBIT_LEAN_CASES(X) \
+    X(17, 1, 1) X(29, 2, 1) X(33, 2, 2) X(49, 3, 2) X(61, 4, 2) X(65, 4, 3) X(80, 5, 3)
+
+// Threads of a lean launch: slices x columns, rounded to 512 or 1024 (the
+// finisher of the streamed orbit works in batches of its block size, which
+// must divide 1024).
+__host__ __device__ constexpr int orbit_lean_threads(int L)
+{
+    return kOrbitLeanSlices * (L + 3) <= 512 ? 512 : 1024;
+}
+
+template <int MAXP, int NSLOT>
+__global__ void __launch_bounds__(1024) orbit_kernel_lean(OrbitLaunch p)
+{
     unsigned smid = 0;
     if (p.sm_busy) {
         asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
@@ -357,7 +594,7 @@ __global__ void __launch_bounds__(kOrbitThreads) orbit_kernel(OrbitLaunch p)
         if (threadIdx.x == 0)
             atomicAdd(p.sm_busy + smid, 1);
     }
-    orbit_produce(p, nullptr);
+    orbit_produce_lean<MAXP, NSLOT>(p, nullptr);
     if (p.sm_busy && threadIdx.x == 0)
         atomicSub(p.sm_busy + smid, 1);
 }
@@ -437,8 +674,9 @@ __device__ __noinline__ void finish_entry(const OrbitLaunch& p, int k, bool from
             p.fe[k] = fmv == 0.0 ? -100000 : fev;
         }
     }
-    // |Z_k|^2 exactly as the pixel loop forms |z|^2 when dz vanishes in FP32
-    p.zq[k] = make_float4(fx, fy, fmaf(fx, fx, fy * fy), fold_sign);
+    // 2 Z_k (the step multiplies by it; doubling is exact) and |Z_k|^2
+    // exactly as the pixel loop forms |z|^2 when dz vanishes in FP32
+    p.zq[k] = make_float4(fx + fx, fy + fy, fmaf(fx, fx, fy * fy), fold_sign);
     const double d_approx = vr * vr + vi * vi - 4.0;
     if (fabs(d_approx) > 9.5367431640625e-7 /* 2^-20 */) {
         p.dd[k] = d_approx;
@@ -769,9 +1007,9 @@ template <class T>
 __device__ __forceinline__ void load_z(const PerturbLaunch& p, int m, T& zx, T& zy)
 {
     if (sizeof(T) == 4) {
-        const float4 z = p.zq[m];
-        zx = (T)z.x;
-        zy = (T)z.y;
+        const float4 z = p.zq[m];   // holds 2 Z_m (exact)
+        zx = (T)(0.5f * z.x);
+        zy = (T)(0.5f * z.y);
     } else {
         const double2 zd = p.zd[m];
         const int ze = p.ze[m];
@@ -1259,23 +1497,24 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
             // folded formulas at deep zoom: z = Z_m in FP32 and no fold
             // within reach of dz among these entries, so the fold keeps
             // Z_m's side; same values as the general step with s = 0
+            // with 2 Z from the orbit copy: 2Z t is Z (2t) exactly
+            T Z2x = Zx + Zx, Z2y = Zy + Zy;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const T tr = st.tr, ti = st.ti;
-                const T u2 = tr + tr, v2 = ti + ti;
                 const T g = grow * magT;
                 if (FR == MDZ_BURNING_SHIP) {
-                    st.tr = Mant<T>::fma_(Zx, u2, Mant<T>::fma_(-Zy, v2, st.dcr));
-                    st.ti = Mant<T>::fma_(fs, Mant<T>::fma_(Zx, v2, Zy * u2), st.dci);
+                    st.tr = Mant<T>::fma_(Z2x, tr, Mant<T>::fma_(-Z2y, ti, st.dcr));
+                    st.ti = Mant<T>::fma_(fs, Mant<T>::fma_(Z2x, ti, Z2y * tr), st.dci);
                 } else {
-                    st.tr = Mant<T>::fma_(fs, Mant<T>::fma_(Zx, u2, -Zy * v2), st.dcr);
-                    st.ti = Mant<T>::fma_(Zx, v2, Mant<T>::fma_(Zy, u2, st.dci));
+                    st.tr = Mant<T>::fma_(fs, Mant<T>::fma_(Z2x, tr, -Z2y * ti), st.dcr);
+                    st.ti = Mant<T>::fma_(Z2x, ti, Mant<T>::fma_(Z2y, tr, st.dci));
                 }
                 st.e2 = Mant<T>::fma_(g, st.e2, Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti));
                 ++m;
                 const float4 q = p.zq[m];
-                Zx = (T)q.x;
-                Zy = (T)q.y;
+                Z2x = (T)q.x;
+                Z2y = (T)q.y;
                 magT = (T)q.z;
                 fs = (T)q.w;
                 if (magT > band_lo || magT < (T)Mant<T>::kGlitchZ2) {
@@ -1284,6 +1523,8 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 }
                 ++wz;
             }
+            Zx = (T)0.5 * Z2x;
+            Zy = (T)0.5 * Z2y;
             // the current z for the fold test of the general step (= Z_m)
             zr = Mant<T>::fma_(st.s, st.tr, Zx);
             zi = Mant<T>::fma_(st.s, st.ti, Zy);
@@ -1312,28 +1553,33 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                    && (!st.slow_if_tiny || four_not_tiny(p, m))) {
             // iterations wz .. wz+3, orbit entries m+1 .. m+4 all finished
             if (st.s == (T)0 && p.att && five_clear(p.att, m)) {
+                const int mstart = m;
                 // deep zoom and none of Z_m .. Z_{m+4} needs attention
                 // (escape band, rebase screen, tiny |Z|): whole blocks of
                 // four run with no test inside, their four orbit loads issued
                 // together; the values are those of the checked block below
                 // (the checks it makes would all have passed)
+                // iteration wz steps from entry m, so wz - m stays fixed: both
+                // bounds (wz + 3 <= last, m + 4 < avail) become one on m
+                const int span = (int)min(last - wz, 0x3fffffffu);
+                const int mmax = min(span + m - 3, avail - 5);
+                T Z2x = Zx + Zx, Z2y = Zy + Zy;
                 do {
                     const float4 q1 = p.zq[m + 1], q2 = p.zq[m + 2], q3 = p.zq[m + 3],
                                  q4 = p.zq[m + 4];
-                    const T zx[4] = {Zx, (T)q1.x, (T)q2.x, (T)q3.x};
-                    const T zy[4] = {Zy, (T)q1.y, (T)q2.y, (T)q3.y};
+                    const T zx[4] = {Z2x, (T)q1.x, (T)q2.x, (T)q3.x};
+                    const T zy[4] = {Z2y, (T)q1.y, (T)q2.y, (T)q3.y};
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
+                        // t' = 2 Z t + dc 2^-e (as the checked block: 2Z t = Z (2t))
                         const T tr = st.tr, ti = st.ti;
-                        const T u2 = tr + tr, v2 = ti + ti;
-                        st.tr = Mant<T>::fma_(zx[u], u2, Mant<T>::fma_(-zy[u], v2, st.dcr));
-                        st.ti = Mant<T>::fma_(zx[u], v2, Mant<T>::fma_(zy[u], u2, st.dci));
+                        st.tr = Mant<T>::fma_(zx[u], tr, Mant<T>::fma_(-zy[u], ti, st.dcr));
+                        st.ti = Mant<T>::fma_(zx[u], ti, Mant<T>::fma_(zy[u], tr, st.dci));
                     }
-                    Zx = (T)q4.x;
-                    Zy = (T)q4.y;
+                    Z2x = (T)q4.x;
+                    Z2y = (T)q4.y;
                     magT = (T)q4.z;
                     m += 4;
-                    wz += 4;
                     // wz - 1 = 4k + 4: the rescale check of the general path
                     const T amax = fmax(fabs(st.tr), fabs(st.ti));
                     if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
@@ -1343,9 +1589,13 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                         st.ti *= sc;
                         st.e += k;
                         refresh_scale(st, dcf_r, dcf_i, dce);
+                        if (st.s != (T)0 || st.force_slow)
+                            break;
                     }
-                } while (st.s == (T)0 && !st.force_slow && wz + 3u <= last && m + 4 < avail
-                         && five_clear(p.att, m));
+                } while (m <= mmax && five_clear(p.att, m));
+                wz += (uint32_t)(m - mstart);
+                Zx = (T)0.5 * Z2x;
+                Zy = (T)0.5 * Z2y;
                 // as a resumed pixel computes it
                 zr = Mant<T>::fma_(st.s, st.tr, Zx);
                 zi = Mant<T>::fma_(st.s, st.ti, Zy);
@@ -1357,16 +1607,16 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 // |Z_m|^2 (stored with the entry, formed as below) and the
                 // rebase screen is |z| tiny -- the same values the general
                 // code computes with s = 0
+                T Z2x = Zx + Zx, Z2y = Zy + Zy;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const T tr = st.tr, ti = st.ti;
-                    const T u2 = tr + tr, v2 = ti + ti;
-                    st.tr = Mant<T>::fma_(Zx, u2, Mant<T>::fma_(-Zy, v2, st.dcr));
-                    st.ti = Mant<T>::fma_(Zx, v2, Mant<T>::fma_(Zy, u2, st.dci));
+                    st.tr = Mant<T>::fma_(Z2x, tr, Mant<T>::fma_(-Z2y, ti, st.dcr));
+                    st.ti = Mant<T>::fma_(Z2x, ti, Mant<T>::fma_(Z2y, tr, st.dci));
                     ++m;
                     const float4 q = p.zq[m];
-                    Zx = (T)q.x;
-                    Zy = (T)q.y;
+                    Z2x = (T)q.x;
+                    Z2y = (T)q.y;
                     magT = (T)q.z;
                     if (magT > band_lo || magT < (T)Mant<T>::kGlitchZ2) {
                         attention = true;
@@ -1374,6 +1624,8 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                     }
                     ++wz;
                 }
+                Zx = (T)0.5 * Z2x;
+                Zy = (T)0.5 * Z2y;
             } else {
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
@@ -1434,6 +1686,8 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                     if (kTrack)
                         magT = Mant<T>::fma_(zr, zr, zi * zi);
                     ++r.rebases;
+                    if (!kTrack && r.rebases > kFp32RebaseLimit)
+                        r.lost = fmaxf(r.lost, 64.f);
                 }
             }
             const bool careful = st.careful && (st.force_slow || z_tiny<T>(p, m, Zx, Zy));
@@ -1521,6 +1775,8 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 if (kTrack)
                     magT = Mant<T>::fma_(zr, zr, zi * zi);
                 ++r.rebases;
+                if (!kTrack && r.rebases > kFp32RebaseLimit)
+                    r.lost = fmaxf(r.lost, 64.f);
                 ++wz;
                 continue;
             }
@@ -1866,11 +2122,13 @@ __global__ void __launch_bounds__(256, FR == MDZ_MANDELBROT ? 5 : 4)
 
 // ---- streamed orbit: pixels start while the orbit is being iterated ----
 
-// Block 0: the producer (kOrbitThreads threads); block 1: the finisher.
-// Launched cooperatively (both blocks resident at once: the finisher waits,
-// bounded, on the producer's progress).
-__global__ void __launch_bounds__(kOrbitThreads) orbit_stream_kernel(OrbitLaunch o, OrbitProgress g,
-                                                           int* producer_sm, DoneSignal done)
+// Block 0: the producer (the lean form for the orbit's digit count); block
+// 1: the finisher (batches of blockDim.x entries).  Launched cooperatively
+// (both blocks resident at once: the finisher waits, bounded, on the
+// producer's progress).
+template <int MAXP, int NSLOT>
+__global__ void __launch_bounds__(1024) orbit_stream_kernel(OrbitLaunch o, OrbitProgress g,
+                                                            int* producer_sm, DoneSignal done)
 {
     if (blockIdx.x == 0) {
         unsigned smid = 0;
@@ -1880,7 +2138,7 @@ __global__ void __launch_bounds__(kOrbitThreads) orbit_stream_kernel(OrbitLaunch
                 atomicAdd(o.sm_busy + smid % (unsigned)o.sm_words, 1);
             *(volatile int*)producer_sm = (int)smid + 1;
         }
-        orbit_produce(o, &g);
+        orbit_produce_lean<MAXP, NSLOT>(o, &g);
         if (threadIdx.x == 0) {
             *(volatile int*)producer_sm = 0;
             if (o.sm_busy)
@@ -2084,8 +2342,14 @@ int launch_orbit_stream(const OrbitLaunch& o, int* progress, cudaStream_t s, Don
     OrbitProgress g{progress + 1, progress + 2, progress + 3, progress + 4};
     int* producer_sm = progress + 5;
     void* args[] = {&oo, &g, &producer_sm, &done};
-    MDZ_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)orbit_stream_kernel, dim3(2),
-                                             dim3(kOrbitThreads), args, 0, s));
+    const void* fn = nullptr;
+#define MDZ_CASE(lmax, mp, ns)                                      \
+    if (!fn && o.limbs <= lmax)                                     \
+        fn = (const void*)orbit_stream_kernel<mp, ns>;
+    MDZ_ORBIT_LEAN_CASES(MDZ_CASE)
+#undef MDZ_CASE
+    MDZ_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(2), dim3(orbit_lean_threads(o.limbs)),
+                                             args, 0, s));
     return MDZGPU_OK;
 }
 
@@ -2134,7 +2398,14 @@ int launch_orbit(const OrbitLaunch& p, cudaStream_t s)
         set_error("orbit: %d limbs outside [5, %d]", p.limbs, kMaxOrbitLimbs);
         return MDZGPU_ERR_UNSUPPORTED;
     }
-    orbit_kernel<<<1, kOrbitThreads, 0, s>>>(p);
+    bool launched = false;
+#define MDZ_CASE(lmax, mp, ns)                                                   \
+    if (!launched && p.limbs <= lmax) {                                          \
+        orbit_kernel_lean<mp, ns><<<1, orbit_lean_threads(p.limbs), 0, s>>>(p); \
+        launched = true;                                                         \
+    }
+    MDZ_ORBIT_LEAN_CASES(MDZ_CASE)
+#undef MDZ_CASE
     MDZ_CUDA_TRY(cudaGetLastError());
     orbit_finish_kernel<<<(p.max_k + 1 + 127) / 128, 128, 0, s>>>(p);
     MDZ_CUDA_TRY(cudaGetLastError());
@@ -2236,9 +2507,13 @@ int preload_perturb_kernels()
     if (!rc)
         rc = preload_fr<MDZ_GENERALIZED_CELTIC>();
     cudaFuncAttributes a;
-    if (!rc && (cudaFuncGetAttributes(&a, orbit_stream_kernel) != cudaSuccess
-                || cudaFuncGetAttributes(&a, orbit_kernel) != cudaSuccess
-                || cudaFuncGetAttributes(&a, orbit_finish_kernel) != cudaSuccess
+#define MDZ_CASE(lmax, mp, ns)                                                        \
+    if (!rc && (cudaFuncGetAttributes(&a, orbit_stream_kernel<mp, ns>) != cudaSuccess \
+                || cudaFuncGetAttributes(&a, orbit_kernel_lean<mp, ns>) != cudaSuccess)) \
+        rc = MDZGPU_ERR_CUDA;
+    MDZ_ORBIT_LEAN_CASES(MDZ_CASE)
+#undef MDZ_CASE
+    if (!rc && (cudaFuncGetAttributes(&a, orbit_finish_kernel) != cudaSuccess
                 || cudaFuncGetAttributes(&a, frame_step_reset_kernel) != cudaSuccess
                 || cudaFuncGetAttributes(&a, serve_enqueue_kernel) != cudaSuccess
                 || cudaFuncGetAttributes(&a, serve_enqueue_count_kernel) != cudaSuccess

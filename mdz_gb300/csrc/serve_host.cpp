@@ -378,6 +378,9 @@ struct Server {
     double rate_adj[kServeClasses];
     double class_ms[kServeClasses] = {};  // summed slice kernel time
     double graph_ms = 0, lead_ms = 0;     // device step spans; begin to first slice
+    // per step: host wall time (graph launch to synchronisation) minus the
+    // device span of the step (its first to its last kernel)
+    std::vector<float> step_gap_ms;
     double loop_ms[9] = {};  // host loop: cancels, admit, orbits, step, finish, idle;
                              // inside step: before the graph, start_finish, graph launch
     long inflight[kServeClasses] = {};   // admitted pixels per class
@@ -875,6 +878,8 @@ int Server::step()
                 first = std::min(first, status_h->tk[cur][c][0]);
         if (b1 > b0) {
             graph_ms += (double)(b1 - b0) * 1e-6;
+            if (step_gap_ms.size() < (1u << 20))
+                step_gap_ms.push_back((float)(t1 - t0 - (double)(b1 - b0) * 1e-6));
             if (first != ~0ull && first > b0)
                 lead_ms += (double)(first - b0) * 1e-6;
         }
@@ -1317,8 +1322,15 @@ void Server::teardown()
                 "\"step_start_finish\": %.1f, \"graph_launch\": %.1f}, ",
                 loop_ms[0], loop_ms[1], loop_ms[2], loop_ms[3], loop_ms[4], loop_ms[5],
                 loop_ms[6], loop_ms[7], loop_ms[8]);
-        fprintf(log, "\"device_step_ms\": %.3f, \"step_lead_ms\": %.3f, \"slice_kernel_ms\": [",
-                graph_ms, lead_ms);
+        fprintf(log, "\"device_step_ms\": %.3f, \"step_lead_ms\": %.3f, ", graph_ms, lead_ms);
+        if (!step_gap_ms.empty()) {
+            std::vector<float> g = step_gap_ms;
+            std::sort(g.begin(), g.end());
+            auto q = [&](double f) { return g[(size_t)(f * (double)(g.size() - 1))]; };
+            fprintf(log, "\"step_gap_ms\": {\"n\": %zu, \"min\": %.4f, \"p10\": %.4f, "
+                    "\"p50\": %.4f, \"p90\": %.4f}, ", g.size(), q(0.0), q(0.1), q(0.5), q(0.9));
+        }
+        fprintf(log, "\"slice_kernel_ms\": [");
         for (int c = 0; c < kServeClasses; ++c)
             fprintf(log, "%s%.3f", c ? ", " : "", class_ms[c]);
         fprintf(log, "], \"rate_adjust\": [");
