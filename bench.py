@@ -45,8 +45,11 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 VIEWS = json.loads((ROOT / "tests" / "golden" / "views.json").read_text())
-# FP32 ops of one perturbation step: complex 2 Z dz (4 mul + 2 add), dz^2
-# (3 mul + 2 add), two adds of dc, |z|^2 (2) and its compare
+# FP32 operations (flops) of one perturbation step: complex 2 Z dz (4 mul +
+# 2 add), dz^2 (3 mul + 2 add), two adds of dc, |z|^2 (2) and its compare.
+# At 2^-1000 the dz^2 terms vanish exactly and the step executes as 4 FFMA
+# (8 flops); the roofline counts the algorithmic 16 against the FP32 flop
+# peak (2 flops per FFMA lane).
 ALGO_OPS_PER_PIXEL_ITER = 16
 # rows of the frame rendered by the plain multi-limb kernel: 1920 x 64 pixels
 # = 3840 warps of 8x4-pixel tiles, about three full waves of the resident
@@ -477,6 +480,7 @@ def run_ours(args, view, world, rank, local, dist):
     # intervals around each launch, on the stream it runs on
     avg_pixel_ms = sum(pixel_ms) / len(pixel_ms)
     achieved = (its / args.steps) * ALGO_OPS_PER_PIXEL_ITER / (avg_pixel_ms * 1e-3) / 1e9
+    peak_gflops = 2.0 * peak.value / 1e9     # FFMA lane-instructions/s x 2 flops
     line = {
         "metric": "pixel-iters/s at 2^-1000 zoom", "value": value, "unit": "pixel-iters/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -491,9 +495,12 @@ def run_ours(args, view, world, rank, local, dist):
         "e2e": {"value": e2e_its_all / (e2e_max * 1e-3), "unit": "pixel-iters/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp32-pipe", "kernel": "perturb_step_kernel",
-                     "achieved": achieved, "peak": peak.value / 1e9,
-                     "unit": "Gop/s", "frac": achieved / (peak.value / 1e9),
-                     "peak_source": "mdzgpu_measure_peak FFMA microbenchmark (this run)",
+                     "achieved": achieved, "peak": peak_gflops,
+                     "unit": "GFLOP/s", "frac": achieved / peak_gflops,
+                     "algorithmic_flops_per_pixel_iter": ALGO_OPS_PER_PIXEL_ITER,
+                     "executed_frac": achieved * 8 / ALGO_OPS_PER_PIXEL_ITER / peak_gflops,
+                     "peak_source": "mdzgpu_measure_peak FFMA microbenchmark (this run), "
+                                    "2 flops per FFMA",
                      "pixel_pass_ms_per_step": avg_pixel_ms,
                      "pixel_pass_launches_per_step": pixel_launches,
                      "traffic": None},

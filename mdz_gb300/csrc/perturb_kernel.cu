@@ -42,16 +42,17 @@ namespace {
 
 constexpr int kTileW = 8;
 constexpr int kTileH = 4;
-// A pixel of the FP32 pass that rebases more often than this is re-run by
-// the FP64 pass.  Repeated rebases mean its orbit keeps returning to the
-// reference's zero -- a pixel around a minibrot, where the count can hinge
-// on the position of c to far below 2^-24 of its offset (near the edge of
-// the minibrot's cardioid the escape time grows like 1/sqrt(distance)), and
-// the FP32 steps' rounding, equivalent to moving c by ~2^-24 |dc| a step,
-// then shifts it by iterations to thousands of iterations (measured on a
-// 2^-1000 frame centred on a period-402 nucleus: 1.2% of the pixels wrong
-// in FP32, none once re-run in FP64).
-constexpr unsigned kFp32RebaseLimit = 8;
+// A pixel of the FP32 pass that steps from a reference entry at zero
+// (|Z_m|^2 < 2^-120 for m past the orbit's start: the view is centred on a
+// minibrot's nucleus, Z_p = 0) is re-run by the FP64 pass: around a nucleus
+// the count can hinge
+// on the position of c far below 2^-24 of its offset (near the edge of the
+// minibrot's cardioid the escape time grows like 1/sqrt(distance)), and the
+// FP32 steps' rounding, equivalent to moving c by ~2^-24 |dc| a step, then
+// shifts it (measured on a 2^-1000 frame centred on a period-402 nucleus:
+// 1.1% of the pixels off by up to 1.5*10^5 iterations in FP32).  The value
+// is the "bits lost" it records, above the FP32 pass's 1-bit limit.
+constexpr float kFp32AtZeroLost = 64.f;
 constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
 constexpr int kOrbitThreads = 512;  // producer threads (sixteen warps)
 
@@ -1686,11 +1687,14 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                     if (kTrack)
                         magT = Mant<T>::fma_(zr, zr, zi * zi);
                     ++r.rebases;
-                    if (!kTrack && r.rebases > kFp32RebaseLimit)
-                        r.lost = fmaxf(r.lost, 64.f);
                 }
             }
             const bool careful = st.careful && (st.force_slow || z_tiny<T>(p, m, Zx, Zy));
+            // stepping from a reference entry at zero other than the orbit's
+            // start (the view is centred on a minibrot's nucleus, Z_p = 0):
+            // the FP64 pass redoes the pixel (see kFp32AtZeroLost)
+            if (!kTrack && m != 0 && !(kTwo && m == q0) && z_tiny<T>(p, m, Zx, Zy))
+                r.lost = fmaxf(r.lost, kFp32AtZeroLost);
             const T g = kTrack ? grow * magT : (T)0;
             // the hybrid folds on odd iterations only
             if (FR != MDZ_MANDELBROT && (!kVar || (wz & 1u))) {
@@ -1775,8 +1779,6 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 if (kTrack)
                     magT = Mant<T>::fma_(zr, zr, zi * zi);
                 ++r.rebases;
-                if (!kTrack && r.rebases > kFp32RebaseLimit)
-                    r.lost = fmaxf(r.lost, 64.f);
                 ++wz;
                 continue;
             }

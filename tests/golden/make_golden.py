@@ -14,6 +14,7 @@ reference sources exist; the GPU tests only read the committed outputs).
   python tests/golden/make_golden.py c2        # c2_frame.json + c2_rows.npz (full config-2 frame)
   python tests/golden/make_golden.py serve_mdz # mdz/*.mdz + serve_mdz.npz (settings files served)
   python tests/golden/make_golden.py perturb_rebase  # perturb_rebase.npz (2^-1000, rebases at depth)
+  python tests/golden/make_golden.py gmp4      # gmp4_counts.npz (GMP callback, four formulas)
 
 Counts come from the UNMODIFIED reference compiled by oracle/build_ref.sh
 (oracle/_ref/libmdzref_d.so: long double = double, no FMA) driven through its
@@ -121,6 +122,37 @@ def make_c2() -> None:
     np.savez_compressed(GOLD / "c2_rows.npz", rows=rows)
     (GOLD / "c2_frame.json").write_text(json.dumps(meta, indent=1))
     print(f"c2: {ref.shape} iters={meta['pixel_iters']} ({time.time() - t0:.1f}s)")
+
+
+GMP4_VIEWS = {0: ("-0.6", "0.5", "0.3"), 1: ("-1.5", "0", "0.4"), 2: ("-1.1", "0.3", "0.4"),
+              3: ("-0.9", "0.2", "0.4")}
+
+
+def make_gmp4() -> None:
+    """MDZ's GMP callback (fractal_gmp_calculate_line, frac_*_gmp) for all
+    four formulas: a 48x32 view each at 128 bits, rendered by the unmodified
+    reference through rth_*, with the GMP values MDZ's own string conversion
+    leaves in img->gxmin / gymax / gwidth (src/my_mpfr_to_str.c:68) recorded
+    for the drop-in test to hand to the same callback."""
+    out, meta = {}, {}
+    for f, (cx, cy, sz) in GMP4_VIEWS.items():
+        key = f"gmp_f{f}"
+        v = View(key, 48, 32, 1200, cx, cy, sz, precision=128, fractal=f, multi_prec=True,
+                 rounding=False)
+        c1, _ = O.ref_render(v, threads=THREADS)
+        d1 = O.ref_view_dump(v)
+        out[key] = c1
+        meta[key] = dict(v.__dict__, gmp={k: d1[k] for k in ("gxmin", "gymax", "gwidth")})
+        print(f"{key}: {len(np.unique(c1))} distinct counts, {(c1 == 0).mean():.3f} inside")
+    np.savez_compressed(GOLD / "gmp4_counts.npz", **out)
+    (GOLD / "gmp4_views.json").write_text(json.dumps(meta, indent=1, default=str))
+
+
+def _mpf_value(g) -> Fraction:
+    _, prec, size, exp, limbs = g
+    n = abs(size)
+    val = sum(Fraction(l) * Fraction(2) ** (64 * (i - n + exp)) for i, l in enumerate(limbs))
+    return -val if size < 0 else val
 
 
 def make_serve_mdz() -> None:
@@ -859,7 +891,8 @@ def main(argv: list[str]) -> None:
          "perturb": make_perturb, "centres": make_centres, "colour": make_colour,
          "perturb_fold": make_perturb_fold, "perturb_julia": make_perturb_julia,
          "perturb_variant": make_perturb_variant, "c2": make_c2,
-         "serve_mdz": make_serve_mdz, "perturb_rebase": make_perturb_rebase}[w]()
+         "serve_mdz": make_serve_mdz, "perturb_rebase": make_perturb_rebase,
+         "gmp4": make_gmp4}[w]()
 
 
 if __name__ == "__main__":

@@ -109,6 +109,44 @@ def test_mp_dropin_gmp_callback():
         d.close()
 
 
+GMP4 = json.loads((GOLD / "gmp4_views.json").read_text())
+GMP4_COUNTS = np.load(GOLD / "gmp4_counts.npz")
+
+
+def gmp_values(m):
+    """The mpf_t values (precision, signed size, exponent, limbs) MDZ's
+    string conversion left in img->gxmin/gymax/gwidth, as exact values."""
+    g = {}
+    for key in ("gxmin", "gymax", "gwidth"):
+        _, prec, size, exp, limbs = m["gmp"][key]
+        n = abs(size)
+        val = sum(Fraction(l) * Fraction(2) ** (64 * (i - n + exp)) for i, l in enumerate(limbs))
+        g[key] = MpVal.from_fraction(-val if size < 0 else val, 64 * max(n, 1))
+    return g
+
+
+@pytest.mark.parametrize("name", sorted(GMP4))
+def test_mp_dropin_gmp_callback_each_formula(name):
+    """fractal_gmp_calculate_line for every formula (frac_mandel_gmp,
+    frac_burning_ship_gmp, frac_generalised_celtic_gmp, frac_variant_gmp),
+    fed the GMP values MDZ itself left in the image, against the reference's
+    own GMP render at 128 bits through rth_* (counts for the whole 48x32
+    view)."""
+    m = GMP4[name]
+    v = View.from_dict({k: x for k, x in m.items() if k != "gmp"})
+    d = DropIn(v, gmp_values=gmp_values(m))
+    try:
+        d.render(timeout_s=300)
+        want = GMP4_COUNTS[name]
+        bad = np.argwhere(d.raw != want)
+        for ln, ix in bad[:10]:
+            print(f"{name} ({ix},{ln}): gpu {d.raw[ln, ix]} reference {want[ln, ix]}")
+        assert len(bad) <= max(1, int(0.001 * want.size)), f"{name}: {len(bad)} pixels differ"
+        assert len(np.unique(want)) > 20
+    finally:
+        d.close()
+
+
 def test_mp_line_entry_point():
     v = view_of("gal_polyp")
     d = DropIn(v)
