@@ -227,6 +227,15 @@ int mdzgpu_colour_device(mdzgpu_ctx* ctx, const int32_t* d_counts,
  * exist to test that path. */
 int mdzgpu_set_wait_limit(mdzgpu_ctx* ctx, int32_t polls);
 
+/* No counterpart in the reference.  The pixels (line * W + ix) the last
+ * perturbation render on this context re-ran: those its FP32 pass handed to
+ * the FP64 pass, and those the FP64 pass handed to the multi-limb kernel, in
+ * the order the passes listed them.  Copies at most cap_fp64 / cap_mp indices;
+ * *n_fp64 / *n_mp receive the full counts.  Valid until the next
+ * perturbation render on the context; MDZGPU_ERR_ARG when there is none. */
+int mdzgpu_last_escalations(mdzgpu_ctx* ctx, uint32_t* fp64, int64_t cap_fp64, int64_t* n_fp64,
+                            uint32_t* mp, int64_t cap_mp, int64_t* n_mp);
+
 /* Largest `words` value the MP kernel is built for. */
 int32_t mdzgpu_mp_max_words(void);
 

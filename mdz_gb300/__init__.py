@@ -155,6 +155,18 @@ class Renderer:
                                                   C.byref(st)))
         return out, (mag if want_mag else None), st.as_dict()
 
+    def last_escalations(self) -> tuple[np.ndarray, np.ndarray]:
+        """Pixel indices (line * W + ix) the last render_perturb re-ran in
+        FP64 and in the multi-limb kernel (mdzgpu_last_escalations)."""
+        n1, n2 = C.c_int64(), C.c_int64()
+        _check(self.lib.mdzgpu_last_escalations(self.ctx, None, 0, C.byref(n1), None, 0,
+                                                C.byref(n2)))
+        a = np.zeros(max(n1.value, 1), np.uint32)
+        b = np.zeros(max(n2.value, 1), np.uint32)
+        _check(self.lib.mdzgpu_last_escalations(self.ctx, a.ctypes.data, n1.value, C.byref(n1),
+                                                b.ctypes.data, n2.value, C.byref(n2)))
+        return a[:n1.value], b[:n2.value]
+
     def render_perturb_device(self, W, H, depth, cx, cy, width, precision, d_out_ptr: int,
                               d_mag_ptr: int | None = None, limbs: int = 0):
         f = Frame(W, H, 0, 0, depth)

@@ -906,6 +906,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     p.stop = nullptr;
     p.spin_limit = ctx->wait_limit;
     // escalation lists: [count1 | count2 | pad] list1[n] list2[n]
+    ctx->esc_pixels = 0;
     if ((rc = ctx->lists.ensure(256 + 2 * n * sizeof(unsigned)))) {
         cudaEventDestroy(evo);
         return rc;
@@ -1032,8 +1033,38 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         st->pixel_ms = pixel_ms;
         st->pixel_launches = pixel_launches;
     }
+    if (!rc)
+        ctx->esc_pixels = (int64_t)n;
     cudaEventDestroy(evo);
     return rc;
+}
+
+int mdzgpu_last_escalations(mdzgpu_ctx* ctx, uint32_t* fp64, int64_t cap_fp64, int64_t* n_fp64,
+                            uint32_t* mp, int64_t cap_mp, int64_t* n_mp)
+{
+    if (!ctx || !n_fp64 || !n_mp || cap_fp64 < 0 || cap_mp < 0 || (cap_fp64 && !fp64)
+        || (cap_mp && !mp)) {
+        set_error("escalations: null argument or negative capacity");
+        return MDZGPU_ERR_ARG;
+    }
+    if (!ctx->esc_pixels) {
+        set_error("escalations: no perturbation render on this context");
+        return MDZGPU_ERR_ARG;
+    }
+    const int64_t n = ctx->esc_pixels;
+    unsigned cnt[2] = {0, 0};
+    MDZ_CUDA_TRY(cudaMemcpyAsync(cnt, ctx->lists.ptr, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    MDZ_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    const unsigned* list1 = (const unsigned*)((const char*)ctx->lists.ptr + 256);
+    const int64_t k1 = std::min<int64_t>(cnt[0], cap_fp64), k2 = std::min<int64_t>(cnt[1], cap_mp);
+    if (k1)
+        MDZ_CUDA_TRY(cudaMemcpyAsync(fp64, list1, k1 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (k2)
+        MDZ_CUDA_TRY(cudaMemcpyAsync(mp, list1 + n, k2 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    MDZ_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *n_fp64 = cnt[0];
+    *n_mp = cnt[1];
+    return MDZGPU_OK;
 }
 
 int mdzgpu_reference_orbit(mdzgpu_ctx* ctx, const mdzgpu_mpval* cx, const mdzgpu_mpval* cy,

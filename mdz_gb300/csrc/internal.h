@@ -102,6 +102,9 @@ struct mdzgpu_ctx {
     // polls a bounded device wait makes before it gives up (mdz::kSpinLimit
     // unless mdzgpu_set_wait_limit changed it)
     int wait_limit = 1 << 25;
+    // pixels of the last perturbation render (its escalation lists sit in
+    // `lists`); 0 when no list is current
+    int64_t esc_pixels = 0;
 };
 
 namespace mdz {

@@ -1692,9 +1692,16 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
             const bool careful = st.careful && (st.force_slow || z_tiny<T>(p, m, Zx, Zy));
             // stepping from a reference entry at zero other than the orbit's
             // start (the view is centred on a minibrot's nucleus, Z_p = 0):
-            // the FP64 pass redoes the pixel (see kFp32AtZeroLost)
-            if (!kTrack && m != 0 && !(kTwo && m == q0) && z_tiny<T>(p, m, Zx, Zy))
+            // the FP64 pass redoes the pixel (see kFp32AtZeroLost), so this
+            // pass stops here
+            if (!kTrack && m != 0 && !(kTwo && m == q0) && z_tiny<T>(p, m, Zx, Zy)) {
                 r.lost = fmaxf(r.lost, kFp32AtZeroLost);
+                if (p.flag_out) {
+                    r.mag = 0.f;
+                    count = 0;
+                    return 1;
+                }
+            }
             const T g = kTrack ? grow * magT : (T)0;
             // the hybrid folds on odd iterations only
             if (FR != MDZ_MANDELBROT && (!kVar || (wz & 1u))) {

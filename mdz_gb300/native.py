@@ -109,6 +109,7 @@ _SIGS = {
                                          C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "mdzgpu_perturb_limbs": (C.c_int32, [C.c_int64]),
     "mdzgpu_set_wait_limit": (C.c_int, [P, C.c_int32]),
+    "mdzgpu_last_escalations": (C.c_int, [P, P, C.c_int64, P, P, C.c_int64, P]),
     "mdzgpu_reference_orbit_formula": (C.c_int, [P, C.c_int32, C.POINTER(MpValStruct),
                                                  C.POINTER(MpValStruct), C.c_int64, C.c_int32,
                                                  C.c_int64, P, P, P, P,

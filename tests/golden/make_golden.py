@@ -130,20 +130,28 @@ GMP4_VIEWS = {0: ("-0.6", "0.5", "0.3"), 1: ("-1.5", "0", "0.4"), 2: ("-1.1", "0
 
 def make_gmp4() -> None:
     """MDZ's GMP callback (fractal_gmp_calculate_line, frac_*_gmp) for all
-    four formulas: a 48x32 view each at 128 bits, rendered by the unmodified
-    reference through rth_*, with the GMP values MDZ's own string conversion
-    leaves in img->gxmin / gymax / gwidth (src/my_mpfr_to_str.c:68) recorded
-    for the drop-in test to hand to the same callback."""
+    four formulas: a 48x32 view each, rendered by the unmodified reference
+    through rth_* at 128 bits and, to confirm the counts, at 256 bits; the
+    GMP values MDZ's own string conversion leaves in img->gxmin / gymax /
+    gwidth at 128 bits (src/my_mpfr_to_str.c:68) are recorded for the
+    drop-in test to hand to the same callback.  A pixel whose count changes
+    with the precision (the burning ship's real axis, where the row's y is
+    a rounding residue that the fold doubles each step) is unconfirmed."""
     out, meta = {}, {}
     for f, (cx, cy, sz) in GMP4_VIEWS.items():
         key = f"gmp_f{f}"
         v = View(key, 48, 32, 1200, cx, cy, sz, precision=128, fractal=f, multi_prec=True,
                  rounding=False)
+        v2 = View(key, 48, 32, 1200, cx, cy, sz, precision=256, fractal=f, multi_prec=True,
+                  rounding=False)
         c1, _ = O.ref_render(v, threads=THREADS)
+        c2, _ = O.ref_render(v2, threads=THREADS)
         d1 = O.ref_view_dump(v)
         out[key] = c1
+        out[key + "__2p"] = c2
         meta[key] = dict(v.__dict__, gmp={k: d1[k] for k in ("gxmin", "gymax", "gwidth")})
-        print(f"{key}: {len(np.unique(c1))} distinct counts, {(c1 == 0).mean():.3f} inside")
+        print(f"{key}: {len(np.unique(c1))} distinct counts, {(c1 == 0).mean():.3f} inside, "
+              f"{int((c1 != c2).sum())} unconfirmed")
     np.savez_compressed(GOLD / "gmp4_counts.npz", **out)
     (GOLD / "gmp4_views.json").write_text(json.dumps(meta, indent=1, default=str))
 

@@ -131,17 +131,18 @@ def test_mp_dropin_gmp_callback_each_formula(name):
     frac_burning_ship_gmp, frac_generalised_celtic_gmp, frac_variant_gmp),
     fed the GMP values MDZ itself left in the image, against the reference's
     own GMP render at 128 bits through rth_* (counts for the whole 48x32
-    view)."""
+    view): equal on every pixel the 256-bit render confirms, and on at least
+    99.9% of them all (or the confirmed fraction, where lower)."""
     m = GMP4[name]
     v = View.from_dict({k: x for k, x in m.items() if k != "gmp"})
     d = DropIn(v, gmp_values=gmp_values(m))
     try:
         d.render(timeout_s=300)
-        want = GMP4_COUNTS[name]
-        bad = np.argwhere(d.raw != want)
-        for ln, ix in bad[:10]:
-            print(f"{name} ({ix},{ln}): gpu {d.raw[ln, ix]} reference {want[ln, ix]}")
-        assert len(bad) <= max(1, int(0.001 * want.size)), f"{name}: {len(bad)} pixels differ"
+        want, want2 = GMP4_COUNTS[name], GMP4_COUNTS[name + "__2p"]
+        for ln, ix in np.argwhere(d.raw != want)[:10]:
+            print(f"{name} ({ix},{ln}): gpu {d.raw[ln, ix]} reference {want[ln, ix]} "
+                  f"at 256 bits {want2[ln, ix]}")
+        check(d.raw, want, want2, name)
         assert len(np.unique(want)) > 20
     finally:
         d.close()
