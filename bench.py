@@ -51,6 +51,13 @@ VIEWS = json.loads((ROOT / "tests" / "golden" / "views.json").read_text())
 # (8 flops); the roofline counts the algorithmic 16 against the FP32 flop
 # peak (2 flops per FFMA lane).
 ALGO_OPS_PER_PIXEL_ITER = 16
+# DRAM bytes (read + written) of one perturb_step_kernel launch of the
+# 1920x1080 2^-1000 frame: ncu dram__bytes_read.sum + dram__bytes_write.sum
+# (one pass, --clock-control none) over launches 61-63 of one frame, 74.7 MB
+# read and 11.6-14.6 MB written each (profiles/perturb_step_kernel_c4_traffic.md).
+# The pixel state (32 B per unfinished pixel) goes in and out once a launch;
+# the reference orbit (3.2 MB of float4 entries) is read from L2.
+STEP_LAUNCH_DRAM_BYTES = 87.6e6
 # rows of the frame rendered by the plain multi-limb kernel: 1920 x 64 pixels
 # = 3840 warps of 8x4-pixel tiles, about three full waves of the resident
 # warps at 34 words (240 registers: 8 warps per SM x 152 SMs)
@@ -313,6 +320,20 @@ def latency_summary(lat: np.ndarray) -> dict:
             "max": float(lat.max()), "mean": float(lat.mean())}
 
 
+def tail_phases(sts: list, lat: np.ndarray) -> dict:
+    """Where the slowest tenth of the requests spent their time: submission
+    to the end of the main pass, waiting for the escalation passes, and in
+    them (means, ms), with their flagged pixel counts."""
+    cut = float(np.percentile(lat, 90, method="inverted_cdf"))
+    sel = [s for s, x in zip(sts, lat) if x >= cut]
+    def mean(k):
+        return float(np.mean([s[k] for s in sel])) if sel else None
+    return {"from_ms": cut, "n": len(sel), "main_ms": mean("main_ms"),
+            "esc_wait_ms": mean("esc_wait_ms"), "esc_ms": mean("esc_ms"),
+            "escalated_fp64": mean("escalated_fp64"), "escalated_mp": mean("escalated_mp"),
+            "with_escalation": sum(1 for s in sel if s["escalated_fp64"] > 0)}
+
+
 def run_serving(args, local) -> dict:
     """The mixed request stream through the serving engine: the first
     `serve_capacity_requests` requests closed loop (all submitted at once)
@@ -380,6 +401,7 @@ def run_serving(args, local) -> dict:
         "latency_ms": latency_summary(lat),
         "latency_ms_by_size": {k: latency_summary(lat[sizes == k]) for k in sorted(set(sizes))},
         "latency_ms_by_method": {k: latency_summary(lat[meth == k]) for k in sorted(set(meth))},
+        "latency_tail": tail_phases(sts2, lat),
         "results_equal_across_runs": same,
         "steps": stats2["steps"], "gpu_launches": stats2["launches"],
         "step_loop": {"host_ms": busy, "device_ms": dev,
@@ -503,7 +525,10 @@ def run_ours(args, view, world, rank, local, dist):
                                     "2 flops per FFMA",
                      "pixel_pass_ms_per_step": avg_pixel_ms,
                      "pixel_pass_launches_per_step": pixel_launches,
-                     "traffic": None},
+                     "traffic": STEP_LAUNCH_DRAM_BYTES,
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read+write)",
+                     "traffic_gbs": STEP_LAUNCH_DRAM_BYTES
+                     / (avg_pixel_ms / max(pixel_launches, 1) * 1e-3) / 1e9},
         "clocks": clocks.summary(),
         "plain_mp": plain,
         "perturb_vs_plain": (value / world / plain["value"]) if plain else None,

@@ -401,6 +401,9 @@ typedef struct mdzgpu_request_status {
     int64_t pixel_iters;          /* sum over pixels of (count ? count : depth) */
     int64_t escalated_fp64, escalated_mp, rebases;
     int64_t steps;                /* engine steps the request took part in */
+    double main_ms;               /* submission -> main pass finished */
+    double esc_wait_ms;           /* main pass -> escalation passes started */
+    double esc_ms;                /* escalation passes (0 when none ran) */
 } mdzgpu_request_status;
 
 typedef struct mdzgpu_serve_stats {

@@ -149,6 +149,8 @@ struct Req {
     bool cancel = false;
     int cancel_state = MDZGPU_REQ_CANCELLED;
     double t_submit = 0, t_admit = 0, t_done = 0;
+    // main pass finished; escalation passes started / ended (0: none)
+    double t_main = 0, t_esc0 = 0, t_esc1 = 0;
     int64_t pixel_iters = 0, esc_fp64 = 0, esc_mp = 0, rebases = 0, steps = 0;
     cudaEvent_t ev_done = nullptr;
     unsigned flagged = 0;        // pixels the FP32 pass sent to the escalation passes
@@ -599,13 +601,17 @@ void Server::end(const std::shared_ptr<Req>& r, int state, int error)
                     "\"formula\": \"%s\", \"depth\": %u, \"method\": \"%s\", \"words\": %d, "
                     "\"pixel_iters\": %lld, \"queue_ms\": %.3f, \"latency_ms\": %.3f, "
                     "\"pixel_iters_per_s\": %.6g, \"escalated_fp64\": %lld, "
-                    "\"escalated_mp\": %lld, \"steps\": %lld}\n",
+                    "\"escalated_mp\": %lld, \"steps\": %lld, \"main_ms\": %.3f, "
+                    "\"esc_wait_ms\": %.3f, \"esc_ms\": %.3f}\n",
                     (long long)r->id, r->W, r->H, r->precision, formula_name(r->fractal),
                     r->depth, r->method == MDZGPU_METHOD_PERTURB ? "perturbation" : "multi_limb",
                     r->method == MDZGPU_METHOD_PERTURB ? r->limbs : r->words,
                     (long long)r->pixel_iters, r->t_admit - r->t_submit, lat,
                     lat > 0 ? (double)r->pixel_iters / (lat * 1e-3) : 0.0,
-                    (long long)r->esc_fp64, (long long)r->esc_mp, (long long)r->steps);
+                    (long long)r->esc_fp64, (long long)r->esc_mp, (long long)r->steps,
+                    r->t_main > 0 ? r->t_main - r->t_submit : 0.0,
+                    r->t_esc0 > 0 ? r->t_esc0 - r->t_main : 0.0,
+                    r->t_esc1 > 0 ? r->t_esc1 - r->t_esc0 : 0.0);
             fflush(log);
         }
     } else if (state == MDZGPU_REQ_FAILED) {
@@ -956,6 +962,7 @@ int Server::start_finish(const std::shared_ptr<Req>& r)
     // the step that finished the FP32 pass reported how many it flagged
     const unsigned flagged = r->method == MDZGPU_METHOD_PERTURB ? status_h->flagged[r->slot] : 0u;
     r->flagged = flagged;
+    r->t_main = wall_ms();
     if (flagged != 0) {
         esc_fifo.push_back(r);
         r->phase = kEscWait;
@@ -1115,6 +1122,7 @@ int Server::advance_finishing()
             rc = launch_escalation(r, true);
         } else if (v == 3) {
             esc_cur = nullptr;
+            r->t_esc1 = wall_ms();
             rc = enqueue_copies(r);
         }
         if (rc) {
@@ -1139,6 +1147,7 @@ int Server::advance_finishing()
             esc_cur = r;
             r->phase = kEscFp64;
             r->esc_base = 0;
+            r->t_esc0 = wall_ms();
             if (int rc = launch_escalation(r, false)) {
                 esc_cur = nullptr;
                 end(r, MDZGPU_REQ_FAILED, rc);
@@ -1440,6 +1449,9 @@ static void fill_status(const Req& r, mdzgpu_request_status* out)
     out->escalated_mp = r.esc_mp;
     out->rebases = r.rebases;
     out->steps = r.steps;
+    out->main_ms = r.t_main > 0 ? r.t_main - r.t_submit : 0.0;
+    out->esc_wait_ms = r.t_esc0 > 0 ? r.t_esc0 - r.t_main : 0.0;
+    out->esc_ms = r.t_esc1 > 0 ? r.t_esc1 - r.t_esc0 : 0.0;
 }
 
 int mdzgpu_serve_poll(mdzgpu_server* srv, int64_t id, mdzgpu_request_status* out)

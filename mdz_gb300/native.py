@@ -65,7 +65,8 @@ class RequestStatus(C.Structure):
     _fields_ = [("state", C.c_int32), ("error", C.c_int32), ("method", C.c_int32),
                 ("words", C.c_int32), ("queue_ms", C.c_double), ("latency_ms", C.c_double),
                 ("pixel_iters", C.c_int64), ("escalated_fp64", C.c_int64),
-                ("escalated_mp", C.c_int64), ("rebases", C.c_int64), ("steps", C.c_int64)]
+                ("escalated_mp", C.c_int64), ("rebases", C.c_int64), ("steps", C.c_int64),
+                ("main_ms", C.c_double), ("esc_wait_ms", C.c_double), ("esc_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

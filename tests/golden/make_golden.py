@@ -124,7 +124,7 @@ def make_c2() -> None:
     print(f"c2: {ref.shape} iters={meta['pixel_iters']} ({time.time() - t0:.1f}s)")
 
 
-GMP4_VIEWS = {0: ("-0.6", "0.5", "0.3"), 1: ("-1.5", "0", "0.4"), 2: ("-1.1", "0.3", "0.4"),
+GMP4_VIEWS = {0: ("-0.6", "0.5", "0.3"), 1: ("-1.5", "0", "0.4"), 2: ("-1.3", "0.2", "0.2"),
               3: ("-0.9", "0.2", "0.4")}
 
 
