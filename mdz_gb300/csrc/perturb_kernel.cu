@@ -852,7 +852,7 @@ struct PixState {
     T tr, ti;       // dz mantissas
     int e;          // dz = t * 2^e
     T s;            // 2^e (0 below the range)
-    T s2x4;         // 4 * 2^(2e), 0 when 2^(2e) underflows
+    T s2scr;        // (1 + 2^-16) 2^(2e): the rebase screen; 0 when 2^(2e) underflows
     T dcr, dci;     // dc * 2^-e
     bool careful;   // slow_if_tiny || force_slow
     bool slow_if_tiny;
@@ -869,7 +869,7 @@ template <class T>
 __device__ __forceinline__ void refresh_scale(PixState<T>& st, T dcm_r, T dcm_i, int dce)
 {
     st.s = Mant<T>::scale((T)1, st.e);
-    st.s2x4 = st.e >= Mant<T>::kSqExp ? (T)4 * st.s * st.s : (T)0;
+    st.s2scr = st.e >= Mant<T>::kSqExp ? (T)1.0000152587890625 * st.s * st.s : (T)0;
     st.dcr = Mant<T>::scale(dcm_r, dce - st.e);
     st.dci = Mant<T>::scale(dcm_i, dce - st.e);
     st.slow_if_tiny = st.e < Mant<T>::kSlowExp;
@@ -1274,7 +1274,7 @@ __device__ __forceinline__ bool wait_orbit(const PerturbLaunch& p, BlockOrbitVie
 }
 
 // Resumable state of one pixel: the deltas, the reference index m, the next
-// iteration wz, the bits lost to rebases so far.  (s, s2x4, dc 2^-e and the
+// iteration wz, the bits lost to rebases so far.  (s, s2scr, dc 2^-e and the
 // flags follow from t, e and dc, so they are recomputed on resume and a
 // resumed run is bit-identical to an uninterrupted one.)
 template <class T>
@@ -1484,8 +1484,9 @@ __device__ __forceinline__ OrbitSnap orbit_snapshot(const PerturbLaunch& p)
 //                                         previous iteration's escape test)
 //   t' = t w + dc 2^-e                  (4 FMA: the complex product)
 //   m += 1;  z' = Z_m + s t'  (2 FMA),  |z'|^2 (2)
-//   attention when |z'|^2 > 4 - 2^-14 (escape band) or |z'| <= 2 |dz'|
-//   (the rebase screen; the exact FP64 test decides) or |z'| tiny.
+//   attention when |z'|^2 > 4 - 2^-14 (escape band) or
+//   |z'|^2 <= (1 + 2^-16) |dz'|^2 (the rebase screen; the exact FP64 test
+//   decides) or |z'| tiny.
 // Iterations 4k+1 .. 4k+4 whose orbit entries are all finished run as one
 // unrolled block without the orbit, budget and rescale checks; the block
 // leaves at the first iteration that needs attention and that iteration
@@ -1700,7 +1701,7 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                     zi = Mant<T>::fma_(st.s, st.ti, Zy);
                     magT = Mant<T>::fma_(zr, zr, zi * zi);
                     const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
-                    if (magT > band_lo || Mant<T>::fma_(st.s2x4, dd, -magT) >= (T)0
+                    if (magT > band_lo || Mant<T>::fma_(st.s2scr, dd, -magT) >= (T)0
                         || magT < (T)Mant<T>::kGlitchZ2) {
                         attention = true;
                         break;
@@ -1830,10 +1831,16 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 return 1;
             }
         }
-        // rebase when |Z_m + dz| < |dz|: screened in T as |z| <= 2 |dz| (or
-        // |z| tiny), decided exactly in FP64
+        // rebase when |Z_m + dz| < |dz|, decided exactly in FP64; the screen
+        // in T passes |z|^2 <= (1 + 2^-16) |dz|^2 (or |z| tiny) to it.  Where
+        // the screen stops a pixel, |z| > |dz| and so |Z_m| < 2 |z|: z in T
+        // (Z_m rounded, one FMA) is off by at most 2^-24 (|Z_m| + |z|) a
+        // component, |z|^2 and |dz|^2 by under 2^-20 relative, and the FP64
+        // test would not rebase either.  (Once a pixel has left the
+        // reference, |z| and |dz| are alike in size and a screen as loose
+        // as |z| <= 2 |dz| sent most of its steps through FP64.)
         const T dd = Mant<T>::fma_(st.tr, st.tr, st.ti * st.ti);
-        if (Mant<T>::fma_(st.s2x4, dd, -magT) >= (T)0 || magT < (T)Mant<T>::kGlitchZ2) {
+        if (Mant<T>::fma_(st.s2scr, dd, -magT) >= (T)0 || magT < (T)Mant<T>::kGlitchZ2) {
             const int e0 = st.e;
             if (rebase_fp64<T>(p, m, st, dcf_r, dcf_i, dce, rebase_lost, true)) {
                 if (kTrack)
