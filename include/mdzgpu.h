@@ -128,6 +128,8 @@ typedef struct mdzgpu_stats {
     double pixel_ms;        /* device time of the FP32 pixel-pass launches
                                alone (perturbation; events around each) */
     int64_t pixel_launches; /* FP32 pixel-pass launches (perturbation) */
+    double esc_fp64_ms;     /* device time of the FP64 escalation pass */
+    double esc_mp_ms;       /* device time of the multi-limb escalation pass */
 } mdzgpu_stats;
 
 /* An arbitrary-precision binary value with MPFR's meaning:

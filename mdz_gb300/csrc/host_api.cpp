@@ -941,6 +941,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         return rc;
     }
     // pass 1: FP64 mantissas over the pixels pass 0 flagged
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev_k0, ctx->stream));
     MDZ_CUDA_TRY(cudaMemsetAsync(&((FrameSync*)ctx->sync.ptr)->tile_counter, 0, sizeof(unsigned),
                                  ctx->stream));
     p.list_in = list1;
@@ -953,6 +954,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         return rc;
     }
     // pass 2: the exact multi-limb kernel for what FP64 could not settle
+    MDZ_CUDA_TRY(cudaEventRecord(ctx->ev_k1, ctx->stream));
     {
         const int w = perturb_mp_words((long)precision);
         std::vector<uint32_t> tab((size_t)(f->width + f->height + 2) * w, 0);
@@ -1032,6 +1034,11 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         st->orbit_len = olen;
         st->pixel_ms = pixel_ms;
         st->pixel_launches = pixel_launches;
+        float e64 = 0.f, emp = 0.f;
+        cudaEventElapsedTime(&e64, ctx->ev_k0, ctx->ev_k1);
+        cudaEventElapsedTime(&emp, ctx->ev_k1, ctx->ev1);
+        st->esc_fp64_ms = e64;
+        st->esc_mp_ms = emp;
     }
     if (!rc)
         ctx->esc_pixels = (int64_t)n;

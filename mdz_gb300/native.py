@@ -29,7 +29,8 @@ class Stats(C.Structure):
                 ("d2h_bytes", C.c_int64), ("launches", C.c_int32), ("words", C.c_int32),
                 ("orbit_ms", C.c_double), ("rebases", C.c_int64), ("orbit_len", C.c_int64),
                 ("escalated_fp64", C.c_int64), ("escalated_mp", C.c_int64),
-                ("pixel_ms", C.c_double), ("pixel_launches", C.c_int64)]
+                ("pixel_ms", C.c_double), ("pixel_launches", C.c_int64),
+                ("esc_fp64_ms", C.c_double), ("esc_mp_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
