@@ -47,7 +47,7 @@ double wall_ms()
 }
 
 constexpr size_t kAlign = 256;
-constexpr int kEscShare = 4;       // escalation passes use 1 / kEscShare of the SMs
+constexpr int kEscShare = 2;       // escalation passes use 1 / kEscShare of the SMs
 constexpr unsigned kEscTilesPerSm = 32;  // list tiles (32 pixels) per SM and chunk
 inline size_t al(size_t b)
 {
