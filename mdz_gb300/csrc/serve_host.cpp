@@ -14,8 +14,9 @@
 //     request's budget of iterations (budgets give each running request an
 //     equal share of the step, scaled by the measured slice-kernel times).
 //   all pixels finished -> perturbation with flagged pixels: the FP64 and
-//     multi-limb escalation passes, one request at a time in chunks on the
-//     low-priority esc stream; then, once the orbit launch has ended too,
+//     multi-limb escalation passes, in chunks on one of the low-priority
+//     esc streams (one request at a time on each); then, once the orbit
+//     launch has ended too,
 //     the results are copied to pinned staging, then to the caller's
 //     buffers; the request's memory is released.  The long kernels (orbit,
 //     passes) report their end in pinned host words: nothing is queued
@@ -48,6 +49,7 @@ double wall_ms()
 
 constexpr size_t kAlign = 256;
 constexpr int kEscShare = 2;       // escalation passes use 1 / kEscShare of the SMs
+constexpr int kEscLanes = 2;       // requests whose escalation passes run at once
 constexpr unsigned kEscTilesPerSm = 32;  // list tiles (32 pixels) per SM and chunk
 inline size_t al(size_t b)
 {
@@ -155,6 +157,7 @@ struct Req {
     cudaEvent_t ev_done = nullptr;
     unsigned flagged = 0;        // pixels the FP32 pass sent to the escalation passes
     unsigned esc_base = 0;       // escalation pass: list tiles launched so far
+    int esc_lane = 0;            // escalation stream it runs on
     bool orbit_running = false;  // streamed orbit not yet complete
     bool cancelled = false;      // finishing only to release the memory
 };
@@ -349,17 +352,17 @@ struct Server {
     cudaStream_t main = nullptr;
     cudaStream_t side[kServeSlots] = {};
     // low priority: each request's result copies (fin) and the escalation
-    // passes of all requests, one after another (esc), on at most
-    // 1 / kEscShare of the SMs so that the steps keep the rest
+    // passes (esc: kEscLanes streams, one request's passes at a time on
+    // each), on at most 1 / kEscShare of the SMs together so that the steps
+    // keep the rest
     cudaStream_t fin[kServeSlots] = {};
-    cudaStream_t esc = nullptr;
+    cudaStream_t esc[kEscLanes] = {};
     // No stream command is ever queued behind a long kernel (it would hold
     // a hardware queue shared with other streams, the steps' among them):
     // the orbit and escalation kernels report their end in pinned host
-    // words, and the host queues what follows them.  One escalation pass
-    // runs at a time.
+    // words, and the host queues what follows them.
     std::deque<std::shared_ptr<Req>> esc_fifo;
-    std::shared_ptr<Req> esc_cur;
+    std::shared_ptr<Req> esc_cur[kEscLanes];
     char* stage_dev = nullptr;  // device alias of stage_host
     cudaStream_t branch[kServeClasses] = {};
     cudaEvent_t fork = nullptr, join[kServeClasses] = {};
@@ -461,7 +464,8 @@ int Server::init(const mdzgpu_serve_config* c)
         MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi));
     for (auto& s : fin)
         MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, lo));
-    MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&esc, cudaStreamNonBlocking, lo));
+    for (auto& s : esc)
+        MDZ_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, lo));
     for (auto& s : branch)
         MDZ_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     MDZ_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
@@ -952,9 +956,11 @@ int Server::step()
 
 // Main pass done.  A perturbation request whose FP32 pass flagged pixels
 // queues for the escalation passes (FP64, then multi-limb over what FP64
-// could not settle), which run one request at a time on the low-priority
-// esc stream with 1 / kEscShare of the SMs, so that a request with many
-// flagged pixels delays its own result, not the steps of the others.
+// could not settle), which run on kEscLanes low-priority streams, one
+// request at a time on each, with 1 / kEscShare of the SMs between them, so
+// that a request with many flagged pixels delays its own result, not the
+// steps of the others (nor, with a second lane, every escalation behind
+// it).
 // Every other request waits only for its orbit launch to end (the arena is
 // released only once nothing writes it), then copies its results out.
 int Server::start_finish(const std::shared_ptr<Req>& r)
@@ -987,16 +993,20 @@ int Server::launch_escalation(const std::shared_ptr<Req>& r, bool mp_pass)
     }
     for (const auto& o : slots)
         alone = alone && (!o || o->phase > kRunning);
+    int lanes = 0;
+    for (const auto& e : esc_cur)
+        lanes += e ? 1 : 0;
     mdzgpu_ctx shape;  // the list passes read only the SM count
     shape.device = device;
-    shape.num_sms = alone ? num_sms : std::max(1, num_sms / kEscShare);
+    shape.num_sms = std::max(1, (alone ? num_sms : num_sms / kEscShare) / std::max(1, lanes));
     const unsigned chunk = (unsigned)shape.num_sms * kEscTilesPerSm;
     PerturbLaunch p = req_h[r->slot].pl;
     unsigned* counts_dev = (unsigned*)(db + l.lists);
     unsigned* list1 = (unsigned*)(db + l.lists + 256);
     unsigned* list2 = list1 + r->npix;
     // the sync block (tile counter, exit count at +128) starts at zero
-    MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, esc));
+    cudaStream_t es = esc[r->esc_lane];
+    MDZ_CUDA_TRY(cudaMemsetAsync(db + l.sync, 0, 256, es));
     const DoneSignal done{(unsigned*)(db + l.sync + 128), dflag(r, mp_pass ? 24 : 20)};
     *hflag(r, mp_pass ? 24 : 20) = 0;
     int rc;
@@ -1009,7 +1019,7 @@ int Server::launch_escalation(const std::shared_ptr<Req>& r, bool mp_pass)
         p.done = done;
         p.tile_base = r->esc_base;
         p.tile_limit = chunk;
-        rc = launch_perturb(&shape, p, esc, 1);
+        rc = launch_perturb(&shape, p, es, 1);
     } else {
         MpLaunch q;
         q.W = r->W;
@@ -1034,7 +1044,7 @@ int Server::launch_escalation(const std::shared_ptr<Req>& r, bool mp_pass)
         q.done = done;
         q.tile_base = r->esc_base;
         q.tile_limit = chunk;
-        rc = launch_mp(&shape, q, esc);
+        rc = launch_mp(&shape, q, es);
     }
     r->esc_base += chunk;
     if (!rc) {
@@ -1105,14 +1115,16 @@ int Server::advance_finishing()
         if (int rc = enqueue_copies(r))
             end(r, MDZGPU_REQ_FAILED, rc);
     }
-    // the escalation chunk in flight: 1 = more of the list is left, 3 = the
+    // the escalation chunks in flight: 1 = more of the list is left, 3 = the
     // pass reached the list's end
-    if (esc_cur) {
-        auto r = esc_cur;
+    for (int k = 0; k < kEscLanes; ++k) {
+        if (!esc_cur[k])
+            continue;
+        auto r = esc_cur[k];
         const int v = *hflag(r, r->phase == kEscFp64 ? 20 : 24);
         int rc = MDZGPU_OK;
         if (v != 0 && r->cancelled) {
-            esc_cur = nullptr;   // cancelled: its memory goes once the orbit ended
+            esc_cur[k] = nullptr;   // cancelled: its memory goes once the orbit ended
             r->phase = kCopyWait;
         } else if (v == 1) {
             rc = launch_escalation(r, r->phase == kEscMp);
@@ -1121,18 +1133,20 @@ int Server::advance_finishing()
             r->esc_base = 0;
             rc = launch_escalation(r, true);
         } else if (v == 3) {
-            esc_cur = nullptr;
+            esc_cur[k] = nullptr;
             r->t_esc1 = wall_ms();
             rc = enqueue_copies(r);
         }
         if (rc) {
-            esc_cur = nullptr;
+            esc_cur[k] = nullptr;
             end(r, MDZGPU_REQ_FAILED, rc);
         }
     }
-    // the next one: the least work (flagged pixels x depth) among those
+    // free lanes take the least work (flagged pixels x depth) among those
     // whose orbit ended
-    if (!esc_cur) {
+    for (int k = 0; k < kEscLanes; ++k) {
+        if (esc_cur[k])
+            continue;
         auto best = esc_fifo.end();
         for (auto it = esc_fifo.begin(); it != esc_fifo.end(); ++it) {
             if ((*it)->orbit_running)
@@ -1141,17 +1155,18 @@ int Server::advance_finishing()
                 || (double)(*it)->flagged * (*it)->depth < (double)(*best)->flagged * (*best)->depth)
                 best = it;
         }
-        if (best != esc_fifo.end()) {
-            auto r = *best;
-            esc_fifo.erase(best);
-            esc_cur = r;
-            r->phase = kEscFp64;
-            r->esc_base = 0;
-            r->t_esc0 = wall_ms();
-            if (int rc = launch_escalation(r, false)) {
-                esc_cur = nullptr;
-                end(r, MDZGPU_REQ_FAILED, rc);
-            }
+        if (best == esc_fifo.end())
+            break;
+        auto r = *best;
+        esc_fifo.erase(best);
+        esc_cur[k] = r;
+        r->esc_lane = k;
+        r->phase = kEscFp64;
+        r->esc_base = 0;
+        r->t_esc0 = wall_ms();
+        if (int rc = launch_escalation(r, false)) {
+            esc_cur[k] = nullptr;
+            end(r, MDZGPU_REQ_FAILED, rc);
         }
     }
     return MDZGPU_OK;
@@ -1233,9 +1248,11 @@ void Server::run()
             tb = ta;
             if (step_rc) {
                 // a failed step leaves the device state unknown: fail everything
-                cudaStreamSynchronize(esc);
+                for (int k = 0; k < kEscLanes; ++k) {
+                    cudaStreamSynchronize(esc[k]);
+                    esc_cur[k] = nullptr;
+                }
                 esc_fifo.clear();
-                esc_cur = nullptr;
                 for (auto& s : slots)
                     if (s) {
                         auto keep = s;
@@ -1266,9 +1283,11 @@ void Server::run()
         cudaStreamSynchronize(s);
     for (auto& s : fin)
         cudaStreamSynchronize(s);
-    cudaStreamSynchronize(esc);
+    for (int k = 0; k < kEscLanes; ++k) {
+        cudaStreamSynchronize(esc[k]);
+        esc_cur[k] = nullptr;
+    }
     esc_fifo.clear();
-    esc_cur = nullptr;
     for (auto& s : slots)
         if (s) {
             auto keep = s;
@@ -1313,8 +1332,9 @@ void Server::teardown()
     for (auto& s : fin)
         if (s)
             cudaStreamDestroy(s);
-    if (esc)
-        cudaStreamDestroy(esc);
+    for (auto& s : esc)
+        if (s)
+            cudaStreamDestroy(s);
     if (main)
         cudaStreamDestroy(main);
     cudaFree(arena_dev);
