@@ -1628,6 +1628,25 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 // bounds (wz + 3 <= last, m + 4 < avail) become one on m
                 const int span = (int)min(last - wz, 0x3fffffffu);
                 const int mmax = min(span + m - 3, avail - 5);
+                // the clear run of the attention mask: no bit is set in
+                // [m, nxt); `hit` when bit nxt is set, else nxt ends the last
+                // mask word read.  A block may start at m while m + 4 < nxt
+                // (five_clear(m)), so the loop runs while m <= lim; the run
+                // is extended a word at a time, reading only words that hold
+                // finished entries (nxt < avail; the finisher publishes
+                // whole lines of the mask).
+                const unsigned w0 = __ldg(p.att + (m >> 5)) & (0xffffffffu << (m & 31));
+                bool hit = w0 != 0u;
+                int nxt = hit ? (m & ~31) + __ffs(w0) - 1 : (m & ~31) + 32;
+                auto extend = [&]() {
+                    while (!hit && nxt <= m + 4 && nxt < avail) {
+                        const unsigned w = __ldg(p.att + (nxt >> 5));
+                        hit = w != 0u;
+                        nxt += hit ? __ffs(w) - 1 : 32;
+                    }
+                    return min(mmax, nxt - 5);
+                };
+                int lim = extend();
                 T Z2x = Zx + Zx, Z2y = Zy + Zy;
                 do {
                     const float4 q1 = p.zq[m + 1], q2 = p.zq[m + 2], q3 = p.zq[m + 3],
@@ -1657,7 +1676,9 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                         if (st.s != (T)0 || st.force_slow)
                             break;
                     }
-                } while (m <= mmax && five_clear(p.att, m));
+                    if (m > lim)
+                        lim = extend();
+                } while (m <= lim);
                 wz += (uint32_t)(m - mstart);
                 Zx = (T)0.5 * Z2x;
                 Zy = (T)0.5 * Z2y;
