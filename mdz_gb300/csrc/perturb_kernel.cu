@@ -1648,37 +1648,47 @@ __device__ int perturb_run(const PerturbLaunch& p, PixRun<T>& r, double dcm_r, d
                 };
                 int lim = extend();
                 T Z2x = Zx + Zx, Z2y = Zy + Zy;
-                do {
-                    const float4 q1 = p.zq[m + 1], q2 = p.zq[m + 2], q3 = p.zq[m + 3],
-                                 q4 = p.zq[m + 4];
-                    const T zx[4] = {Z2x, (T)q1.x, (T)q2.x, (T)q3.x};
-                    const T zy[4] = {Z2y, (T)q1.y, (T)q2.y, (T)q3.y};
+                // blocks counted down to the run's end; entries read through
+                // a pointer (immediate offsets); a block after which |t| left
+                // [2^-32, 2^32] ends the loop and the rescale follows it (the
+                // rescale is exact, a power of two: where it happens changes
+                // no value, and the next pass through here carries on)
+                const float4* zp = p.zq + m;
+                bool out = false;
+                for (;;) {
+                    int nb = (lim - m) / 4 + 1;
+                    do {
+                        const float4 q1 = zp[1], q2 = zp[2], q3 = zp[3], q4 = zp[4];
+                        const T zx[4] = {Z2x, (T)q1.x, (T)q2.x, (T)q3.x};
+                        const T zy[4] = {Z2y, (T)q1.y, (T)q2.y, (T)q3.y};
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        // t' = 2 Z t + dc 2^-e (as the checked block: 2Z t = Z (2t))
-                        const T tr = st.tr, ti = st.ti;
-                        st.tr = Mant<T>::fma_(zx[u], tr, Mant<T>::fma_(-zy[u], ti, st.dcr));
-                        st.ti = Mant<T>::fma_(zx[u], ti, Mant<T>::fma_(zy[u], tr, st.dci));
-                    }
-                    Z2x = (T)q4.x;
-                    Z2y = (T)q4.y;
-                    magT = (T)q4.z;
-                    m += 4;
-                    // wz - 1 = 4k + 4: the rescale check of the general path
+                        for (int u = 0; u < 4; ++u) {
+                            // t' = 2 Z t + dc 2^-e (as the checked block: 2Z t = Z (2t))
+                            const T tr = st.tr, ti = st.ti;
+                            st.tr = Mant<T>::fma_(zx[u], tr, Mant<T>::fma_(-zy[u], ti, st.dcr));
+                            st.ti = Mant<T>::fma_(zx[u], ti, Mant<T>::fma_(zy[u], tr, st.dci));
+                        }
+                        Z2x = (T)q4.x;
+                        Z2y = (T)q4.y;
+                        magT = (T)q4.z;
+                        zp += 4;
+                        // wz - 1 = 4k + 4: the rescale check of the general path
+                        const T amax = fmax(fabs(st.tr), fabs(st.ti));
+                        out = (amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0;
+                    } while (--nb > 0 && !out);
+                    m = (int)(zp - p.zq);
+                    if (out || (lim = extend()) < m)
+                        break;
+                }
+                if (out) {
                     const T amax = fmax(fabs(st.tr), fabs(st.ti));
-                    if ((amax > (T)4.2949673e9 || amax < (T)2.3283064e-10) && amax != (T)0) {
-                        const int k = Mant<T>::exponent_of(amax);
-                        const T sc = Mant<T>::scale((T)1, -k);
-                        st.tr *= sc;
-                        st.ti *= sc;
-                        st.e += k;
-                        refresh_scale(st, dcf_r, dcf_i, dce);
-                        if (st.s != (T)0 || st.force_slow)
-                            break;
-                    }
-                    if (m > lim)
-                        lim = extend();
-                } while (m <= lim);
+                    const int k = Mant<T>::exponent_of(amax);
+                    const T sc = Mant<T>::scale((T)1, -k);
+                    st.tr *= sc;
+                    st.ti *= sc;
+                    st.e += k;
+                    refresh_scale(st, dcf_r, dcf_i, dce);
+                }
                 wz += (uint32_t)(m - mstart);
                 Zx = (T)0.5 * Z2x;
                 Zy = (T)0.5 * Z2y;
