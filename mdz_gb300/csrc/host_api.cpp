@@ -956,6 +956,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
     }
     // pass 2: the exact multi-limb kernel for what FP64 could not settle
     MDZ_CUDA_TRY(cudaEventRecord(ctx->ev_k1, ctx->stream));
+    bool mp_skipped = false;
     {
         unsigned n_mp = 0;
         MDZ_CUDA_TRY(cudaMemcpyAsync(&n_mp, counts_dev + 1, 4, cudaMemcpyDeviceToHost,
@@ -974,6 +975,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
             cudaEventDestroy(evo);
             return rc ? rc : MDZGPU_ERR_RANGE;
         }
+        mp_skipped = n_mp == 0;
         if (n_mp == 0) {
             --launches;   // nothing left for the multi-limb kernel
         } else {
@@ -1050,7 +1052,7 @@ static int perturb_common(mdzgpu_ctx* ctx, const mdzgpu_frame* f, const mdzgpu_m
         cudaEventElapsedTime(&e64, ctx->ev_k0, ctx->ev_k1);
         cudaEventElapsedTime(&emp, ctx->ev_k1, ctx->ev1);
         st->esc_fp64_ms = e64;
-        st->esc_mp_ms = emp;
+        st->esc_mp_ms = mp_skipped ? 0.0 : emp;
     }
     if (!rc)
         ctx->esc_pixels = (int64_t)n;
