@@ -202,3 +202,34 @@ def test_python_half_spacing_equals_library():
         cases.append((MpVal.from_fraction(Fraction(num, 1 << 62) * Fraction(2) ** e, prec), W))
     for w, W in cases:
         assert perturb_half_spacing(w, W) == perturb_spacing(w, W), (w, W)
+
+
+# the explicit C API's structs: the ctypes mirrors in mdz_gb300/native.py
+# against the header, field by field (offsets and sizes from gcc)
+NATIVE_STRUCTS = [("Frame", "mdzgpu_frame"), ("Stats", "mdzgpu_stats"),
+                  ("MpValStruct", "mdzgpu_mpval"), ("Palette", "mdzgpu_palette"),
+                  ("ServeConfig", "mdzgpu_serve_config"), ("Request", "mdzgpu_request"),
+                  ("RequestStatus", "mdzgpu_request_status"),
+                  ("ServeStats", "mdzgpu_serve_stats")]
+
+
+def test_native_structs_match_header(tmp_path):
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "mdzgpu.h"', "int main(void) {"]
+    want = []
+    for py, cname in NATIVE_STRUCTS:
+        cls = getattr(native, py)
+        lines.append(f'  printf("%ld\\n", (long)sizeof({cname}));')
+        want.append((cname, "sizeof", C.sizeof(cls)))
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("%ld\\n", (long)offsetof({cname}, {f}));')
+            want.append((cname, f, getattr(cls, f).offset))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "native_layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "native_layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    bad = [(c, f, g, w) for (c, f, w), g in zip(want, got) if g != w]
+    assert len(got) == len(want) and not bad, bad
