@@ -556,26 +556,7 @@ __device__ __forceinline__ void orbit_produce_lean(const OrbitLaunch& p, const O
                 out[pp - 3] = d;
             }
         }
-        if (ship) {
-            summary(pt, (k + 1) & 1);   // also the sign of the part
-        } else {
-            // the escape estimate from the registers: digit L-1 sits in
-            // column L+2, digit L-2 one lane below it (or in lane 31 of the
-            // slot before); the same value summary() reads back from z
-            const int ptop = L + 2, ttop = ptop >> 5, ltop = ptop & 31;
-            float e = 0.f;
-#pragma unroll
-            for (int t = 0; t < NSLOT; ++t) {
-                const int d1 = (int)v[t];
-                const int below = __shfl_up_sync(0xffffffffu, d1, 1);
-                const int wrapd = __shfl_sync(0xffffffffu, t > 0 ? (int)v[t - 1] : 0, 31);
-                const int d2 = lane == 0 ? wrapd : below;
-                if (t == ttop && lane == ltop)
-                    e = fmaf((float)d2, 3.7252903e-9f, (float)d1);
-            }
-            if (lane == ltop)
-                esc[pt][(k + 1) & 1] = e;
-        }
+        summary(pt, (k + 1) & 1);
         if (prog && ((k + 1) & 63) == 0)
             __threadfence();  // Z_{k+1}'s digits before raw_len = k + 2
     }
