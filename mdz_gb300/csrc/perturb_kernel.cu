@@ -44,17 +44,18 @@ constexpr int kTileW = 8;
 constexpr int kTileH = 4;
 // A pixel of the FP32 pass that steps from a reference entry at zero
 // (|Z_m|^2 < 2^-120 for m past the orbit's start: the view is centred on a
-// minibrot's nucleus, Z_p = 0) is re-run by the FP64 pass: around a nucleus
-// the count can hinge
-// on the position of c far below 2^-24 of its offset (near the edge of the
-// minibrot's cardioid the escape time grows like 1/sqrt(distance)), and the
-// FP32 steps' rounding, equivalent to moving c by ~2^-24 |dc| a step, then
-// shifts it (measured on a 2^-1000 frame centred on a period-402 nucleus:
-// 1.1% of the pixels off by up to 1.5*10^5 iterations in FP32).  The value
-// is the "bits lost" it records, above the FP32 pass's 1-bit limit.
+// minibrot's nucleus, Z_p = 0) is handed to the FP64 pass there: around a
+// nucleus the count can hinge on the position of c far below 2^-24 of its
+// offset (near the edge of the minibrot's cardioid the escape time grows
+// like 1/sqrt(distance)), and the FP32 steps' rounding, equivalent to
+// moving c by ~2^-24 |dc| a step, then shifts it (measured on a 2^-1000
+// frame centred on a period-402 nucleus: 1.1% of the pixels off by up to
+// 1.5*10^5 iterations in FP32; an exact restatement of four of them needed
+// ~50 significant bits).  The error estimate does not see it: the local
+// dynamics are near parabolic, errors add rather than grow.  The value is
+// the "bits lost" it records, above the FP32 pass's 1-bit limit.
 constexpr float kFp32AtZeroLost = 64.f;
 constexpr int kMaxOrbitLimbs = 80;  // F up to 2212 bits
-constexpr int kOrbitThreads = 512;  // producer threads (sixteen warps)
 
 // --------------------------------------------------------------------------
 // Reference orbit
