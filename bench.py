@@ -503,6 +503,11 @@ def run_ours(args, view, world, rank, local, dist):
     avg_pixel_ms = sum(pixel_ms) / len(pixel_ms)
     achieved = (its / args.steps) * ALGO_OPS_PER_PIXEL_ITER / (avg_pixel_ms * 1e-3) / 1e9
     peak_gflops = 2.0 * peak.value / 1e9     # FFMA lane-instructions/s x 2 flops
+    traffic_gbs = STEP_LAUNCH_DRAM_BYTES / (avg_pixel_ms / max(pixel_launches, 1) * 1e-3) / 1e9
+    try:
+        hbm_gbs = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs")
+    except (OSError, ValueError):
+        hbm_gbs = None
     line = {
         "metric": "pixel-iters/s at 2^-1000 zoom", "value": value, "unit": "pixel-iters/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -527,8 +532,8 @@ def run_ours(args, view, world, rank, local, dist):
                      "pixel_pass_launches_per_step": pixel_launches,
                      "traffic": STEP_LAUNCH_DRAM_BYTES,
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read+write)",
-                     "traffic_gbs": STEP_LAUNCH_DRAM_BYTES
-                     / (avg_pixel_ms / max(pixel_launches, 1) * 1e-3) / 1e9},
+                     "traffic_gbs": traffic_gbs,
+                     "traffic_frac_of_measured_hbm": (traffic_gbs / hbm_gbs) if hbm_gbs else None},
         "clocks": clocks.summary(),
         "plain_mp": plain,
         "perturb_vs_plain": (value / world / plain["value"]) if plain else None,
